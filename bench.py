@@ -1,0 +1,329 @@
+#!/usr/bin/env python
+"""Benchmark: wavelet + threshold + zero-bits + shuffle + LZ4 compression of a
+512^3 fp32 field on one GB300 (and decompression), through libczgpu.so.
+
+Workload (one step): compress one 512^3 float32 field (200 Gaussian blobs,
+k^-5/3 noise, 12 tanh interfaces; seeded synthetic) = 4096 blocks of 32^3,
+4th-order interpolating wavelets (wtype 1), threshold 1e-3 x (max-min),
+4 mantissa bits zeroed, byte shuffle, LZ4, one record per chunk. The field
+(512 MiB) is larger than L2 (129 MB), so no flush is needed between steps.
+
+  value    compress GB/s of input, field resident in HBM (device timing)
+  e2e      the same through the host-buffer C-ABI call (pinned host field in,
+           .cz image in host memory out; host->device and device->host copies
+           inside the timed region)
+  roofline encode kernel (fwt+threshold+mask+survivors): algorithmic bytes
+           per launch (field read + record bytes written) / its CUDA-event
+           time, against the measured HBM copy bandwidth
+  cpu_baseline  the same compression on the host cores (CPU oracle port)
+
+`--impl reference` times the CPU implementation of the path on the host
+cores (rank 0 only) with the same config and metric.
+
+Multi-GPU (torchrun): every rank compresses its own field (weak scaling, no
+data-path collective); time = max over ranks; value = all ranks' bytes / time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZE = 512
+REL_THR = 1e-3
+WTYPE, ZEROBITS, SHUFFLE = 1, 4, True
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_field(seed):
+    from cubismz_gb300 import synth
+    return synth.generate((SIZE, SIZE, SIZE), seed=seed, blobs=200, interfaces=12)
+
+
+def cpu_port_time(field, eps, threads, max_seconds=20.0):
+    """The CPU oracle port (OpenMP, all host threads) on the same field:
+    returns (seconds per full field, sample description)."""
+    from oracle import czoracle as O
+    t0 = time.perf_counter()
+    O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, 1, threads)
+    dt = time.perf_counter() - t0
+    reps = 1
+    while reps < 3 and (reps + 1) * dt < max_seconds:
+        t0 = time.perf_counter()
+        O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, 1, threads)
+        dt = min(dt, time.perf_counter() - t0)
+        reps += 1
+    return dt, f"full {SIZE}^3 field, best of {reps}"
+
+
+def run_reference(args, rank, world):
+    """CPU implementation of the path on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    from oracle import czoracle as O
+    threads = os.cpu_count() or 1
+    field = make_field(0)
+    eps = float(np.float32(REL_THR * float(field.max() - field.min())))
+    kind = "port"
+    for _ in range(max(0, min(args.warmup, 1))):
+        O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, 1, threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, 1, threads)
+        times.append(time.perf_counter() - t0)
+    dt = float(np.mean(times))
+    gbs = field.nbytes / dt / 1e9
+    line = {
+        "impl": "reference", "metric": "compress GB/s @512^3 fp32", "value": gbs, "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"compress {SIZE}^3 fp32 field, wtype 1, thr 1e-3*range, zerobits 4, shuffle, lz4",
+                   "threads": threads},
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": kind,
+                         "sample": f"full {SIZE}^3 field per step"},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import cubismz_gb300 as cz
+    from cubismz_gb300 import _lib
+    import ctypes as C
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    field = make_field(rank)
+    fmin, fmax = float(field.min()), float(field.max())
+    eps = float(np.float32(REL_THR * (fmax - fmin)))
+    f_dev = torch.from_numpy(field).to(dev)
+    ctx = cz.context(local_rank)
+    nbytes = field.nbytes
+    stream = torch.cuda.current_stream(dev)
+
+    def compress():
+        return cz.compress_field(f_dev, eps, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
+
+    for _ in range(args.warmup):
+        cf = compress()
+    torch.cuda.synchronize()
+
+    # ---- device-resident compress (the headline `value`)
+    ctx.set_timing(True)
+    enc_ms, lz_ms, asm_ms = [], [], []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local_rank) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            cf = compress()
+            st = ctx.stage_times()
+            enc_ms.append(st[0])
+            lz_ms.append(st[1])
+            asm_ms.append(st[2])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ctx.set_timing(False)
+    ms = t0.elapsed_time(t1) / args.steps
+    if dist:
+        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    comp_bytes = cf.nbytes
+    raw_bytes = cf.raw_bytes
+
+    # ---- decompress (device resident)
+    data, off = cf.to_device()
+    out = torch.empty_like(f_dev)
+    for _ in range(max(1, args.warmup)):
+        cz.decompress_field(data, off, field.shape, WTYPE, SHUFFLE, encoder="lz4", out=out)
+    torch.cuda.synchronize()
+    d0 = torch.cuda.Event(enable_timing=True)
+    d1 = torch.cuda.Event(enable_timing=True)
+    d0.record(stream)
+    for _ in range(args.steps):
+        cz.decompress_field(data, off, field.shape, WTYPE, SHUFFLE, encoder="lz4", out=out)
+    d1.record(stream)
+    torch.cuda.synchronize()
+    dms = d0.elapsed_time(d1) / args.steps
+    dec = out.cpu().numpy()
+    err = np.abs(dec.astype(np.float64) - field)
+    mse = float((err * err).mean())
+    psnr = 20 * np.log10((fmax - fmin) / (2 * np.sqrt(mse))) if mse > 0 else float("inf")
+
+    # ---- end to end through the host-buffer C-ABI call
+    h_field = torch.from_numpy(field).pin_memory()
+    cap = (nbytes // (32 ** 3 * 4)) * (4 + _lib.MAX_RECORD + 16) * 2 + 65536
+    h_out = torch.empty(cap, dtype=torch.uint8).pin_memory()
+    prm = cz.params(eps, WTYPE, ZEROBITS, SHUFFLE, "lz4", 1)
+    w = C.c_longlong(0)
+
+    def e2e_once():
+        ctx.check(ctx.L.cz_compress_to_image(ctx.h, C.c_void_p(h_field.data_ptr()), SIZE, SIZE, SIZE, C.byref(prm),
+                                             C.c_void_p(stream.cuda_stream), C.c_void_p(h_out.data_ptr()), cap,
+                                             C.byref(w)))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_once()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_once()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - te) / args.steps
+    if dist:
+        tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    image_bytes = w.value
+
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel (encode)
+    peak, peak_kind = peaks()
+    enc = float(np.mean(enc_ms))
+    alg = nbytes + raw_bytes  # field read + records written, per launch
+    achieved = alg / (enc * 1e-3) / 1e9
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "encode_kernel_traffic.json")
+    if os.path.exists(tr_path):
+        with open(tr_path) as f:
+            traffic = json.load(f).get("traffic_bytes_per_launch_512")
+    # ---- CPU baseline (oracle port, all host cores, same field)
+    threads = os.cpu_count() or 1
+    cpu_s, sample = cpu_port_time(field, eps, threads)
+    line = {
+        "metric": "compress GB/s @512^3 fp32", "value": world * nbytes / (ms * 1e-3) / 1e9, "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded 512^3 field per rank)",
+        "config": {"workload": f"compress {SIZE}^3 fp32 field per GPU: wtype 1, thr {REL_THR}*range, zerobits 4, "
+                               f"shuffle, lz4, 1 record per chunk",
+                   "field_bytes": nbytes, "l2": "inputs larger than L2 (512 MiB field)",
+                   "parallelism": f"replicas x{world}"},
+        "compression": {"ratio": nbytes / image_bytes, "cz_bytes": image_bytes, "payload_bytes": comp_bytes,
+                        "pre_lz4_bytes": raw_bytes, "psnr_db": psnr, "max_abs_err": float(err.max())},
+        "stages_ms": {"encode_kernel": enc, "lz4": float(np.mean(lz_ms)), "assembly": float(np.mean(asm_ms))},
+        "decompress": {"value": world * nbytes / (dms * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": dms},
+        "e2e": {"value": world * nbytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": image_bytes},
+        "roofline": {"bound": "hbm", "kernel": "encode_kernel", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "algorithmic_bytes": alg, "peak_source": peak_kind},
+        "cpu_baseline": {"value": nbytes / cpu_s / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "gpu_launches": 7 * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

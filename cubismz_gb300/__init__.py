@@ -1,0 +1,13 @@
+"""cubismz_gb300: GB300-native wavelet compression path of CubismZ.
+
+The compute path is libczgpu.so (hand-written CUDA for sm_103a behind the C
+ABI in include/czgpu.h); this package is its Python binding and mirrors the
+reference compressor interface (see api.py).
+"""
+from .api import (Context, CompressedField, WaveletCompressor, compress_field, compress_to_image, context,
+                  decompress_field, decompress_image, image_info, lz4_compress, lz4_decompress, params)
+from ._lib import CzError
+
+__all__ = ["Context", "CompressedField", "WaveletCompressor", "compress_field", "compress_to_image", "context",
+           "decompress_field", "decompress_image", "image_info", "lz4_compress", "lz4_decompress", "params",
+           "CzError"]

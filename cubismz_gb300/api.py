@@ -1,0 +1,242 @@
+"""Python mirror of the reference compressor interface over libczgpu.so.
+
+The names follow the reference: WaveletCompressor mirrors
+WaveletCompressorGeneric<32,float> (Compressor/source/WaveletCompressor.h:35-94):
+uncompressed_data(), compress(threshold, float16, wtype), compressed_data(),
+decompress(float16, nbytes, wtype). Field-level calls take torch CUDA
+tensors (device memory) or numpy arrays (host memory); torch is plumbing for
+device memory and streams only. Errors raise CzError, as the reference
+aborts.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import CzError, Params, Stream
+
+_CTX = {}
+
+
+class Context:
+    """One libczgpu context (device scratch buffers grow on demand)."""
+
+    def __init__(self, device=0):
+        self.L = _lib.load()
+        h = C.c_void_p()
+        rc = self.L.cz_create(device, C.byref(h))
+        if rc != 0:
+            raise CzError(rc, f"cz_create({device}) failed (no CUDA device?)")
+        self.h = h
+        self.device = device
+
+    def check(self, rc):
+        if rc != 0:
+            raise CzError(rc, self.L.cz_last_error(self.h).decode(errors="replace"))
+
+    def set_timing(self, on=True):
+        self.check(self.L.cz_set_timing(self.h, 1 if on else 0))
+
+    def stage_times(self):
+        """Per-stage device times (ms) of the last field call."""
+        out = (C.c_float * 3)()
+        n = self.L.cz_stage_times(self.h, out, 3)
+        return list(out)[:max(n, 0)]
+
+    def close(self):
+        if self.h:
+            self.L.cz_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def context(device=0):
+    """Process-wide context per device."""
+    if device not in _CTX:
+        _CTX[device] = Context(device)
+    return _CTX[device]
+
+
+def params(eps, wtype=1, zerobits=0, shuffle=False, encoder="none", blocks_per_chunk=1):
+    enc = {"none": _lib.ENCODER_NONE, "lz4": _lib.ENCODER_LZ4}[encoder] if isinstance(encoder, str) else int(encoder)
+    return Params(float(eps), int(wtype), int(zerobits), 1 if shuffle else 0, enc, int(blocks_per_chunk))
+
+
+def _u8(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint8))
+
+
+def _f32(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class WaveletCompressor:
+    """Per-block drop-in for WaveletCompressorGeneric<32,float>: the same
+    method names and buffer semantics; compression runs on the GPU.
+    zerobits/shuffle are the reference's build options (-D_ZEROBITS_,
+    -D_USE_SHUFFLE3_) given at construction."""
+
+    def __init__(self, zerobits=0, shuffle=False, device=0):
+        self.ctx = context(device)
+        self.zerobits = zerobits
+        self.shuffle = shuffle
+        self._data = np.zeros((32, 32, 32), np.float32)
+        self._buf = np.zeros(_lib.MAX_RECORD, np.uint8)
+
+    def uncompressed_data(self):
+        return self._data
+
+    def compressed_data(self):
+        return self._buf
+
+    def compress(self, threshold, float16=False, wtype=1):
+        n = C.c_int(0)
+        d = np.ascontiguousarray(self._data, np.float32)
+        self.ctx.check(self.ctx.L.cz_block_compress(self.ctx.h, _f32(d), C.c_float(threshold), int(wtype),
+                                                    self.zerobits, 1 if self.shuffle else 0, _u8(self._buf),
+                                                    C.byref(n)))
+        return n.value
+
+    def decompress(self, float16, nbytes, wtype, out=None):
+        dst = np.zeros((32, 32, 32), np.float32) if out is None else out
+        self.ctx.check(self.ctx.L.cz_block_decompress(self.ctx.h, _u8(self._buf), int(nbytes), int(wtype),
+                                                      1 if self.shuffle else 0, _f32(dst)))
+        self._data[...] = dst
+        return dst
+
+
+def lz4_compress(data, device=0):
+    """LZ4_compress on the GPU (host bytes in, host bytes out)."""
+    ctx = context(device)
+    src = np.frombuffer(bytes(data), np.uint8).copy()
+    cap = ctx.L.cz_lz4_bound(src.size)
+    dst = np.zeros(max(cap, 1), np.uint8)
+    n = C.c_int(0)
+    ctx.check(ctx.L.cz_lz4_compress(ctx.h, _u8(src) if src.size else None, src.size, _u8(dst), cap, C.byref(n)))
+    return dst[: n.value].tobytes()
+
+
+def lz4_decompress(data, cap, device=0):
+    """LZ4_uncompress_unknownOutputSize semantics; raises CzError on
+    malformed input."""
+    ctx = context(device)
+    src = np.frombuffer(bytes(data), np.uint8).copy()
+    dst = np.zeros(max(cap, 1), np.uint8)
+    n = C.c_int(0)
+    rc = ctx.L.cz_lz4_decompress(ctx.h, _u8(src) if src.size else None, src.size, _u8(dst), cap, C.byref(n))
+    ctx.check(rc)
+    return dst[: n.value].tobytes()
+
+
+class CompressedField:
+    """A compressed field in the context's device buffers (valid until the
+    next call on the same context)."""
+
+    def __init__(self, ctx, stream, shape, prm):
+        self.ctx, self.s, self.shape, self.params = ctx, stream, shape, prm
+
+    @property
+    def nbytes(self):
+        return self.s.data_bytes
+
+    @property
+    def raw_bytes(self):
+        return self.s.raw_bytes
+
+    def to_device(self, stream=None):
+        """Copy the compressed chunks and their offsets (rebased to 0) into
+        new CUDA tensors (uint8 data, int64 offsets)."""
+        import torch
+        dev = f"cuda:{self.ctx.device}"
+        data = torch.empty(max(self.s.data_bytes, 1), dtype=torch.uint8, device=dev)
+        off = torch.empty(self.s.nchunks + 1, dtype=torch.int64, device=dev)
+        st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+        self.ctx.check(self.ctx.L.cz_stream_copy(self.ctx.h, C.byref(self.s), C.c_void_p(data.data_ptr()),
+                                                 C.c_void_p(off.data_ptr()), C.c_void_p(st)))
+        return data[: self.s.data_bytes], off
+
+    def image(self):
+        """The .cz file image (host bytes)."""
+        nz, ny, nx = self.shape
+        cap = self.ctx.L.cz_file_bytes(self.ctx.h, C.byref(self.s), nx, ny, nz, C.byref(self.params))
+        out = np.empty(cap, np.uint8)
+        w = C.c_longlong(0)
+        self.ctx.check(self.ctx.L.cz_file_image(self.ctx.h, C.byref(self.s), nx, ny, nz, C.byref(self.params),
+                                                out.ctypes.data, cap, C.byref(w)))
+        return out[: w.value].tobytes()
+
+
+def compress_field(field, eps, wtype=1, zerobits=0, shuffle=False, encoder="lz4", blocks_per_chunk=1, stream=None):
+    """Compress a CUDA tensor field of shape (nz, ny, nx), x fastest."""
+    import torch
+    assert field.is_cuda and field.dtype == torch.float32 and field.is_contiguous()
+    nz, ny, nx = field.shape
+    ctx = context(field.device.index or 0)
+    prm = params(eps, wtype, zerobits, shuffle, encoder, blocks_per_chunk)
+    s = Stream()
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(field.device).cuda_stream
+    ctx.check(ctx.L.cz_field_compress(ctx.h, C.c_void_p(field.data_ptr()), nx, ny, nz, C.byref(prm),
+                                      C.c_void_p(st), C.byref(s)))
+    return CompressedField(ctx, s, (nz, ny, nx), prm)
+
+
+def decompress_field(data, offsets, shape, wtype=1, shuffle=False, encoder="lz4", blocks_per_chunk=1, out=None,
+                     stream=None):
+    """Decompress device chunks (uint8 tensor + int64 offsets tensor) into a
+    CUDA field of the given (nz, ny, nx) shape."""
+    import torch
+    nz, ny, nx = shape
+    dev = data.device
+    ctx = context(dev.index or 0)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float32, device=dev)
+    prm = params(0.0, wtype, 0, shuffle, encoder, blocks_per_chunk)
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    ctx.check(ctx.L.cz_field_decompress(ctx.h, C.c_void_p(data.data_ptr()), C.c_void_p(offsets.data_ptr()),
+                                        offsets.numel() - 1, nx, ny, nz, C.byref(prm), C.c_void_p(st),
+                                        C.c_void_p(out.data_ptr())))
+    return out
+
+
+def compress_to_image(field, eps, wtype=1, zerobits=0, shuffle=False, encoder="lz4", device=0, out=None):
+    """Host field (numpy, (nz, ny, nx)) -> .cz image bytes, end to end. `out`
+    may be a preallocated host uint8 buffer (pinned for full speed); the
+    image is then returned as a view of it."""
+    ctx = context(device)
+    f = np.ascontiguousarray(field, np.float32)
+    nz, ny, nx = f.shape
+    prm = params(eps, wtype, zerobits, shuffle, encoder, 1)
+    nblocks = (nx // 32) * (ny // 32) * (nz // 32)
+    cap = nblocks * (4 + _lib.MAX_RECORD + 16) * 2 + 65536
+    buf = out if out is not None else np.empty(cap, np.uint8)
+    w = C.c_longlong(0)
+    ctx.check(ctx.L.cz_compress_to_image(ctx.h, f.ctypes.data, nx, ny, nz, C.byref(prm), None, buf.ctypes.data,
+                                         buf.size, C.byref(w)))
+    return buf[: w.value]
+
+
+def image_info(img):
+    L = _lib.load()
+    a = np.frombuffer(bytes(img), np.uint8)
+    dims = (C.c_int * 3)()
+    enc = C.c_int(-1)
+    rc = L.cz_image_info(a.ctypes.data, a.size, dims, C.byref(enc))
+    if rc != 0:
+        raise CzError(rc, "not a .cz image")
+    return (dims[2], dims[1], dims[0]), enc.value
+
+
+def decompress_image(img, wtype=1, shuffle=False, device=0):
+    """.cz image bytes -> host field (numpy, (nz, ny, nx))."""
+    ctx = context(device)
+    a = np.frombuffer(bytes(img), np.uint8)
+    shape, _ = image_info(a)
+    out = np.empty(shape, np.float32)
+    ctx.check(ctx.L.cz_decompress_image(ctx.h, a.ctypes.data, a.size, int(wtype), 1 if shuffle else 0, None,
+                                        out.ctypes.data, out.size))
+    return out

@@ -1,0 +1,689 @@
+// cz_api.cu -- the C-ABI of libczgpu.so (include/czgpu.h): context, device
+// buffer management and the compress/decompress pipelines.
+//
+// Compress pipeline (one stream, no host round trip until the final size):
+//   encode_kernel        fwt + threshold + mask + survivors -> block slots
+//   chunk_setup          chunk geometry (blocks_per_chunk records per chunk)
+//   pack_records         (blocks_per_chunk > 1) records back to back per chunk
+//   lz4_encode_kernel    (encoder lz4) one warp per chunk
+//   scan                 chunk offsets (replaces the writer's offset allocation)
+//   gather               chunk payloads back to back
+// Decompress pipeline: decode_setup, lz4_decode_kernel, record location,
+// decode_kernel (load + iwt) straight into the output field.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/czgpu.h"
+#include "cz_codec.h"
+#include "cz_device.cuh"
+#include "cz_format.h"
+
+using namespace cz;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+constexpr long long lz4_bound_ll(long long n) { return n + n / 255 + 16; }
+
+}  // namespace
+
+struct cz_ctx {
+    int device = 0;
+    int sms = 1;
+    std::string err;
+    DevBuf fields, stage, rec_bytes, chunk_in, in_off, in_len, blk_dst, lz_off, lz_out, lz_len, out_off, out_data,
+        queue, status, flag, rec_off, dec, dec_off, dec_cap, dec_len, raw_off, chunk_rec, block_chunk, block_subid,
+        tmp_field, tmp_in;
+    void *pin = nullptr;  // small pinned host scratch
+    size_t pin_cap = 0;
+    // geometry of the last compressed stream
+    long long nblocks = 0;
+    int nchunks = 0, bpc = 1;
+    // stage timing
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float stage_ms[3] = {0, 0, 0};
+};
+
+namespace {
+
+int fail(cz_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CZ_CUDA(ctx, call)                                                                          \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) return fail(ctx, CZ_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+int grow(cz_ctx *c, DevBuf &b, size_t bytes)
+{
+    if (bytes <= b.cap && b.p) return CZ_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    if (cudaMalloc(&b.p, want) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, CZ_E_NOMEM, "device allocation of " + std::to_string(want) + " bytes failed");
+    }
+    b.cap = want;
+    return CZ_OK;
+}
+
+int grow_pin(cz_ctx *c, size_t bytes)
+{
+    if (bytes <= c->pin_cap && c->pin) return CZ_OK;
+    if (c->pin) cudaFreeHost(c->pin);
+    c->pin = nullptr;
+    c->pin_cap = 0;
+    if (cudaMallocHost(&c->pin, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, CZ_E_NOMEM, "pinned host allocation failed");
+    }
+    c->pin_cap = bytes;
+    return CZ_OK;
+}
+
+#define CZ_TRY(x)                  \
+    do {                           \
+        const int r_ = (x);        \
+        if (r_ != CZ_OK) return r_; \
+    } while (0)
+
+template <class T>
+T *P(DevBuf &b)
+{
+    return reinterpret_cast<T *>(b.p);
+}
+
+int check_params(cz_ctx *c, const cz_params *p)
+{
+    if (!p) return fail(c, CZ_E_ARG, "params is NULL");
+    if (p->zerobits < 0 || p->zerobits > 31) return fail(c, CZ_E_ARG, "zerobits must be in [0,31]");
+    if (p->encoder != CZ_ENCODER_NONE && p->encoder != CZ_ENCODER_LZ4)
+        return fail(c, CZ_E_ARG, "encoder must be CZ_ENCODER_NONE or CZ_ENCODER_LZ4");
+    if (p->blocks_per_chunk < 1 || p->blocks_per_chunk > 64) return fail(c, CZ_E_ARG, "blocks_per_chunk must be in [1,64]");
+    if (!(p->eps == p->eps)) return fail(c, CZ_E_ARG, "eps is NaN");
+    return CZ_OK;
+}
+
+int check_dims(cz_ctx *c, int nx, int ny, int nz)
+{
+    if (nx <= 0 || ny <= 0 || nz <= 0 || nx % 32 || ny % 32 || nz % 32)
+        return fail(c, CZ_E_ARG, "field extents must be positive multiples of 32");
+    return CZ_OK;
+}
+
+int set_device(cz_ctx *c)
+{
+    CZ_CUDA(c, cudaSetDevice(c->device));
+    return CZ_OK;
+}
+
+// stage marks k = 0..3 on the call's stream when timing is enabled
+int mark(cz_ctx *c, int k, cudaStream_t st)
+{
+    if (!c->timing) return CZ_OK;
+    if (!c->ev[k]) CZ_CUDA(c, cudaEventCreate(&c->ev[k]));
+    CZ_CUDA(c, cudaEventRecord(c->ev[k], st));
+    return CZ_OK;
+}
+
+// after the call's final synchronisation
+void collect(cz_ctx *c)
+{
+    if (!c->timing) return;
+    for (int k = 0; k < 3; ++k) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]) != cudaSuccess) {
+            cudaGetLastError();
+            ms = -1.f;
+        }
+        c->stage_ms[k] = ms;
+    }
+}
+
+// Runs the compress pipeline over `nfields` descriptors already in host
+// memory; fills the context's stream buffers. Returns after the total size is
+// known (one small device-to-host copy).
+int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const cz_params *p,
+                    cudaStream_t st, cz_stream *out)
+{
+    const int bpc = p->blocks_per_chunk;
+    const long long nch_ll = (nblocks + bpc - 1) / bpc;
+    if (nch_ll > 0x7fffffffLL) return fail(c, CZ_E_ARG, "too many chunks");
+    const int nchunks = (int)nch_ll;
+    const long long lz_slot = (lz4_bound_ll((long long)bpc * kSlotBytes) + 15) / 16 * 16;
+
+    CZ_TRY(grow(c, c->fields, sizeof(CzField) * fields.size()));
+    CZ_TRY(grow(c, c->stage, (size_t)nblocks * kSlotBytes));
+    CZ_TRY(grow(c, c->rec_bytes, sizeof(int) * nblocks));
+    CZ_TRY(grow(c, c->in_off, sizeof(long long) * nchunks));
+    CZ_TRY(grow(c, c->in_len, sizeof(int) * nchunks));
+    CZ_TRY(grow(c, c->lz_off, sizeof(long long) * nchunks));
+    CZ_TRY(grow(c, c->lz_len, sizeof(int) * nchunks));
+    CZ_TRY(grow(c, c->out_off, sizeof(long long) * (nchunks + 1)));
+    CZ_TRY(grow(c, c->raw_off, sizeof(long long) * (nchunks + 1)));
+    CZ_TRY(grow(c, c->queue, 64));
+    CZ_TRY(grow(c, c->flag, 64));
+    if (bpc > 1) {
+        CZ_TRY(grow(c, c->blk_dst, sizeof(long long) * nblocks));
+        CZ_TRY(grow(c, c->chunk_in, (size_t)nchunks * bpc * kSlotBytes));
+    }
+    if (p->encoder == CZ_ENCODER_LZ4) CZ_TRY(grow(c, c->lz_out, (size_t)nchunks * lz_slot));
+    // the gathered stream is bounded by the lossless bound of every chunk
+    const size_t out_cap = (size_t)nchunks * (p->encoder == CZ_ENCODER_LZ4 ? lz_slot : (long long)bpc * kSlotBytes);
+    CZ_TRY(grow(c, c->out_data, out_cap));
+    CZ_TRY(grow_pin(c, std::max<size_t>(4096, sizeof(CzField) * fields.size() + 64)));
+
+    memcpy(c->pin, fields.data(), sizeof(CzField) * fields.size());
+    CZ_CUDA(c, cudaMemcpyAsync(c->fields.p, c->pin, sizeof(CzField) * fields.size(), cudaMemcpyHostToDevice, st));
+    CZ_CUDA(c, cudaMemsetAsync(c->queue.p, 0, 64, st));
+    CZ_CUDA(c, cudaMemsetAsync(c->flag.p, 0, 64, st));
+    const int grid = (int)std::min<long long>(nblocks, c->sms);
+    CZ_TRY(mark(c, 0, st));
+    CZ_CUDA(c, cz_launch_encode(p->wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, p->zerobits,
+                                p->shuffle ? 1 : 0, P<uint8_t>(c->stage), P<int>(c->rec_bytes),
+                                P<unsigned long long>(c->queue), grid, st));
+    CZ_TRY(mark(c, 1, st));
+    CZ_CUDA(c, cz_launch_chunk_setup(bpc, nblocks, nchunks, P<int>(c->rec_bytes), P<long long>(c->in_off),
+                                     P<int>(c->in_len), bpc > 1 ? P<long long>(c->blk_dst) : nullptr,
+                                     P<long long>(c->lz_off), lz_slot, st));
+    const uint8_t *chunk_src = P<uint8_t>(c->stage);
+    if (bpc > 1) {
+        CZ_CUDA(c, cz_launch_pack_records(P<uint8_t>(c->stage), P<int>(c->rec_bytes), nblocks,
+                                          P<long long>(c->blk_dst), P<uint8_t>(c->chunk_in), st));
+        chunk_src = P<uint8_t>(c->chunk_in);
+    }
+    CZ_CUDA(c, cz_launch_scan(P<int>(c->in_len), nchunks, P<long long>(c->raw_off), st));
+    const uint8_t *gsrc = chunk_src;
+    const long long *gsrc_off = P<long long>(c->in_off);
+    const int *glen = P<int>(c->in_len);
+    if (p->encoder == CZ_ENCODER_LZ4) {
+        const int lzgrid = std::max(1, std::min((nchunks + 3) / 4, c->sms * 8));
+        CZ_CUDA(c, cz_launch_lz4_encode(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
+                                        P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<int>(c->lz_len), lzgrid,
+                                        st));
+        CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len), nchunks, P<int>(c->flag), st));
+        gsrc = P<uint8_t>(c->lz_out);
+        gsrc_off = P<long long>(c->lz_off);
+        glen = P<int>(c->lz_len);
+    }
+    CZ_TRY(mark(c, 2, st));
+    CZ_CUDA(c, cz_launch_scan(glen, nchunks, P<long long>(c->out_off), st));
+    CZ_CUDA(c, cz_launch_gather(gsrc, gsrc_off, glen, nchunks, P<uint8_t>(c->out_data), P<long long>(c->out_off), st));
+    CZ_TRY(mark(c, 3, st));
+    long long *h = reinterpret_cast<long long *>(c->pin);
+    CZ_CUDA(c, cudaMemcpyAsync(&h[0], P<long long>(c->out_off) + nchunks, 8, cudaMemcpyDeviceToHost, st));
+    CZ_CUDA(c, cudaMemcpyAsync(&h[1], P<long long>(c->raw_off) + nchunks, 8, cudaMemcpyDeviceToHost, st));
+    CZ_CUDA(c, cudaMemcpyAsync(&h[2], c->flag.p, 4, cudaMemcpyDeviceToHost, st));
+    CZ_CUDA(c, cudaStreamSynchronize(st));
+    collect(c);
+    if (reinterpret_cast<int *>(&h[2])[0] != 0) return fail(c, CZ_E_CUDA, "LZ4 encoder output exceeded its bound");
+    c->nblocks = nblocks;
+    c->nchunks = nchunks;
+    c->bpc = bpc;
+    out->data = P<uint8_t>(c->out_data);
+    out->data_bytes = h[0];
+    out->chunk_offsets = P<long long>(c->out_off);
+    out->nchunks = nchunks;
+    out->nblocks = nblocks;
+    out->raw_bytes = h[1];
+    return CZ_OK;
+}
+
+// Decompress pipeline for a field whose records sit in chunks of bpc
+// consecutive blocks, or (block_chunk != NULL) with an explicit
+// block -> (chunk, subid) map (files written by other writers).
+int decompress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const uint8_t *d_data,
+                      const long long *d_off, int nchunks, int encoder, int wtype, int shuffle, int bpc,
+                      const int *h_block_chunk, const int *h_block_subid, int maxsub, cudaStream_t st)
+{
+    const int per_chunk = h_block_chunk ? maxsub : bpc;
+    const long long dcap = ((long long)per_chunk * (4 + kMaxRecord) + 15) / 16 * 16;
+    CZ_TRY(grow(c, c->fields, sizeof(CzField) * fields.size()));
+    CZ_TRY(grow(c, c->in_len, sizeof(int) * nchunks));
+    CZ_TRY(grow(c, c->dec_off, sizeof(long long) * nchunks));
+    CZ_TRY(grow(c, c->dec_cap, sizeof(int) * nchunks));
+    CZ_TRY(grow(c, c->dec_len, sizeof(int) * nchunks));
+    CZ_TRY(grow(c, c->rec_off, sizeof(long long) * nblocks));
+    CZ_TRY(grow(c, c->status, sizeof(int) * nblocks));
+    CZ_TRY(grow(c, c->queue, 64));
+    CZ_TRY(grow(c, c->flag, 64));
+    if (encoder == CZ_ENCODER_LZ4) CZ_TRY(grow(c, c->dec, (size_t)nchunks * dcap));
+    // pinned scratch: [fields | flag (64 B) | block map]
+    const size_t pin_fields = (sizeof(CzField) * fields.size() + 63) / 64 * 64;
+    const size_t map_bytes = h_block_chunk ? sizeof(int) * 2 * nblocks : 0;
+    CZ_TRY(grow_pin(c, std::max<size_t>(4096, pin_fields + 64 + map_bytes)));
+    memcpy(c->pin, fields.data(), sizeof(CzField) * fields.size());
+    CZ_CUDA(c, cudaMemcpyAsync(c->fields.p, c->pin, sizeof(CzField) * fields.size(), cudaMemcpyHostToDevice, st));
+    CZ_CUDA(c, cudaMemsetAsync(c->queue.p, 0, 64, st));
+    CZ_CUDA(c, cudaMemsetAsync(c->flag.p, 0, 64, st));
+    const int raw = encoder != CZ_ENCODER_LZ4;
+    CZ_TRY(mark(c, 0, st));
+    CZ_CUDA(c, cz_launch_decode_setup(nchunks, d_off, P<int>(c->in_len), P<long long>(c->dec_off), P<int>(c->dec_cap),
+                                      dcap, raw, st));
+    const uint8_t *base = d_data;
+    const int *dlen = P<int>(c->in_len);
+    if (!raw) {
+        const int lzgrid = std::max(1, std::min((nchunks + 3) / 4, c->sms * 8));
+        CZ_CUDA(c, cz_launch_lz4_decode(d_data, d_off, P<int>(c->in_len), nchunks, P<uint8_t>(c->dec),
+                                        P<long long>(c->dec_off), P<int>(c->dec_cap), P<int>(c->dec_len), lzgrid, st));
+        base = P<uint8_t>(c->dec);
+        dlen = P<int>(c->dec_len);
+    }
+    CZ_TRY(mark(c, 1, st));
+    if (h_block_chunk) {
+        CZ_TRY(grow(c, c->chunk_rec, sizeof(long long) * (size_t)nchunks * maxsub));
+        CZ_TRY(grow(c, c->block_chunk, sizeof(int) * nblocks));
+        CZ_TRY(grow(c, c->block_subid, sizeof(int) * nblocks));
+        int *hp = reinterpret_cast<int *>(reinterpret_cast<char *>(c->pin) + pin_fields + 64);
+        memcpy(hp, h_block_chunk, sizeof(int) * nblocks);
+        memcpy(hp + nblocks, h_block_subid, sizeof(int) * nblocks);
+        CZ_CUDA(c, cudaMemcpyAsync(c->block_chunk.p, hp, sizeof(int) * nblocks, cudaMemcpyHostToDevice, st));
+        CZ_CUDA(c, cudaMemcpyAsync(c->block_subid.p, hp + nblocks, sizeof(int) * nblocks, cudaMemcpyHostToDevice, st));
+        const long long *cbase = raw ? d_off : P<long long>(c->dec_off);
+        CZ_CUDA(c, cz_launch_chunk_records(nchunks, maxsub, cbase, dlen, base, P<long long>(c->chunk_rec), st));
+        CZ_CUDA(c, cz_launch_map_blocks(nblocks, nchunks, maxsub, P<int>(c->block_chunk), P<int>(c->block_subid),
+                                        P<long long>(c->chunk_rec), P<long long>(c->rec_off), st));
+    } else {
+        const long long *cbase = raw ? d_off : P<long long>(c->dec_off);
+        CZ_CUDA(c, cz_launch_locate_records(bpc, nblocks, nchunks, cbase, dlen, P<long long>(c->rec_off),
+                                            P<int>(c->status), base, st));
+    }
+    const int grid = (int)std::min<long long>(nblocks, c->sms);
+    CZ_TRY(mark(c, 2, st));
+    CZ_CUDA(c, cz_launch_decode(wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, shuffle ? 1 : 0, base,
+                                P<long long>(c->rec_off), P<int>(c->status), P<unsigned long long>(c->queue), grid,
+                                st));
+    CZ_TRY(mark(c, 3, st));
+    CZ_CUDA(c, cz_launch_status_reduce(P<int>(c->status), nblocks, P<int>(c->flag), st));
+    int *hflag = reinterpret_cast<int *>(reinterpret_cast<char *>(c->pin) + pin_fields);
+    CZ_CUDA(c, cudaMemcpyAsync(hflag, c->flag.p, 4, cudaMemcpyDeviceToHost, st));
+    CZ_CUDA(c, cudaStreamSynchronize(st));
+    collect(c);
+    if (*hflag != 0) return fail(c, CZ_E_CORRUPT, "malformed chunk or record in the compressed stream");
+    return CZ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cz_create(int device, cz_ctx **out)
+{
+    if (!out) return CZ_E_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return CZ_E_CUDA;
+    }
+    cz_ctx *c = new cz_ctx;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return CZ_E_CUDA;
+    }
+    *out = c;
+    return CZ_OK;
+}
+
+int cz_destroy(cz_ctx *c)
+{
+    if (!c) return CZ_OK;
+    cudaSetDevice(c->device);
+    DevBuf *all[] = {&c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
+                     &c->blk_dst, &c->lz_off,  &c->lz_out,    &c->lz_len,    &c->out_off,     &c->out_data,
+                     &c->queue,   &c->status,  &c->flag,      &c->rec_off,   &c->dec,         &c->dec_off,
+                     &c->dec_cap, &c->dec_len, &c->raw_off,   &c->chunk_rec, &c->block_chunk, &c->block_subid,
+                     &c->tmp_field, &c->tmp_in};
+    for (DevBuf *b : all)
+        if (b->p) cudaFree(b->p);
+    for (cudaEvent_t e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->pin) cudaFreeHost(c->pin);
+    delete c;
+    return CZ_OK;
+}
+
+const char *cz_last_error(cz_ctx *c) { return c ? c->err.c_str() : "no context"; }
+
+int cz_set_timing(cz_ctx *c, int on)
+{
+    if (!c) return CZ_E_ARG;
+    c->timing = on != 0;
+    return CZ_OK;
+}
+
+int cz_stage_times(cz_ctx *c, float *ms, int n)
+{
+    if (!c || !ms || n < 0) return CZ_E_ARG;
+    const int k = n < 3 ? n : 3;
+    for (int i = 0; i < k; ++i) ms[i] = c->stage_ms[i];
+    return k;
+}
+
+int cz_field_compress(cz_ctx *c, const float *d_field, int nx, int ny, int nz, const cz_params *p, void *stream,
+                      cz_stream *out)
+{
+    if (!c || !d_field || !out) return fail(c, CZ_E_ARG, "NULL argument");
+    CZ_TRY(check_params(c, p));
+    CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(set_device(c));
+    const long long nblocks = (long long)(nx / 32) * (ny / 32) * (nz / 32);
+    std::vector<CzField> f(1);
+    f[0] = CzField{d_field, nx, ny, nz, p->eps, 0};
+    return compress_fields(c, f, nblocks, p, (cudaStream_t)stream, out);
+}
+
+int cz_stream_copy(cz_ctx *c, const cz_stream *s, uint8_t *d_data, long long *d_off, void *stream)
+{
+    if (!c || !s) return fail(c, CZ_E_ARG, "NULL argument");
+    CZ_TRY(set_device(c));
+    cudaStream_t st = (cudaStream_t)stream;
+    long long base = 0;
+    CZ_CUDA(c, cudaMemcpyAsync(&base, s->chunk_offsets, 8, cudaMemcpyDeviceToHost, st));
+    CZ_CUDA(c, cudaStreamSynchronize(st));
+    if (d_data && s->data_bytes > 0)
+        CZ_CUDA(c, cudaMemcpyAsync(d_data, s->data + base, (size_t)s->data_bytes, cudaMemcpyDeviceToDevice, st));
+    if (d_off) {
+        CZ_CUDA(c, cudaMemcpyAsync(d_off, s->chunk_offsets, sizeof(long long) * (s->nchunks + 1),
+                                   cudaMemcpyDeviceToDevice, st));
+        if (base) CZ_CUDA(c, cz_launch_rebase(d_off, s->nchunks + 1, base, st));
+    }
+    return CZ_OK;
+}
+
+int cz_field_decompress(cz_ctx *c, const uint8_t *d_data, const long long *d_off, int nchunks, int nx, int ny, int nz,
+                        const cz_params *p, void *stream, float *d_field)
+{
+    if (!c || !d_data || !d_off || !d_field) return fail(c, CZ_E_ARG, "NULL argument");
+    CZ_TRY(check_params(c, p));
+    CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(set_device(c));
+    const long long nblocks = (long long)(nx / 32) * (ny / 32) * (nz / 32);
+    const int bpc = p->blocks_per_chunk;
+    if ((long long)nchunks != (nblocks + bpc - 1) / bpc) return fail(c, CZ_E_ARG, "chunk count does not match the field");
+    std::vector<CzField> f(1);
+    f[0] = CzField{d_field, nx, ny, nz, p->eps, 0};
+    return decompress_fields(c, f, nblocks, d_data, d_off, nchunks, p->encoder, p->wtype, p->shuffle, bpc, nullptr,
+                             nullptr, 0, (cudaStream_t)stream);
+}
+
+int cz_batch_compress(cz_ctx *c, int nfields, const float *const *d_fields, const int *dims, const float *eps,
+                      const cz_params *p, void *stream, cz_stream *out)
+{
+    if (!c || nfields <= 0 || !d_fields || !dims || !eps || !out) return fail(c, CZ_E_ARG, "bad batch arguments");
+    CZ_TRY(check_params(c, p));
+    CZ_TRY(set_device(c));
+    std::vector<CzField> f(nfields);
+    long long total = 0;
+    for (int i = 0; i < nfields; ++i) {
+        CZ_TRY(check_dims(c, dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]));
+        if (!d_fields[i]) return fail(c, CZ_E_ARG, "NULL field in batch");
+        f[i] = CzField{d_fields[i], dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], eps[i], total};
+        total += (long long)(dims[3 * i] / 32) * (dims[3 * i + 1] / 32) * (dims[3 * i + 2] / 32);
+    }
+    cz_params q = *p;
+    // chunks never straddle fields: one record per chunk in batched mode
+    q.blocks_per_chunk = 1;
+    cz_stream all;
+    CZ_TRY(compress_fields(c, f, total, &q, (cudaStream_t)stream, &all));
+    // per-field views into the shared stream (chunk c = block c)
+    for (int i = 0; i < nfields; ++i) {
+        const long long nb = (long long)(dims[3 * i] / 32) * (dims[3 * i + 1] / 32) * (dims[3 * i + 2] / 32);
+        out[i].data = all.data;
+        out[i].chunk_offsets = all.chunk_offsets + f[i].block0;
+        out[i].nchunks = (int)nb;
+        out[i].nblocks = nb;
+        out[i].data_bytes = -1;  // per-field sizes: chunk_offsets[nb] - chunk_offsets[0]
+        out[i].raw_bytes = -1;
+    }
+    return CZ_OK;
+}
+
+// ---------------------------------------------------------------- per block
+int cz_block_compress(cz_ctx *c, const float *in, float eps, int wtype, int zerobits, int shuffle, uint8_t *out,
+                      int *nbytes)
+{
+    if (!c || !in || !out || !nbytes) return fail(c, CZ_E_ARG, "NULL argument");
+    CZ_TRY(set_device(c));
+    CZ_TRY(grow(c, c->tmp_field, sizeof(float) * kBS3));
+    CZ_CUDA(c, cudaMemcpy(c->tmp_field.p, in, sizeof(float) * kBS3, cudaMemcpyHostToDevice));
+    cz_params p = {eps, wtype, zerobits, shuffle, CZ_ENCODER_NONE, 1};
+    cz_stream s;
+    CZ_TRY(cz_field_compress(c, P<float>(c->tmp_field), 32, 32, 32, &p, nullptr, &s));
+    int nb = 0;
+    CZ_CUDA(c, cudaMemcpy(&nb, s.data, 4, cudaMemcpyDeviceToHost));
+    if (nb < kMaskBytes || nb > kMaxRecord) return fail(c, CZ_E_CUDA, "record size out of range");
+    CZ_CUDA(c, cudaMemcpy(out, s.data + 4, nb, cudaMemcpyDeviceToHost));
+    *nbytes = nb;
+    return CZ_OK;
+}
+
+int cz_block_decompress(cz_ctx *c, const uint8_t *in, int nbytes, int wtype, int shuffle, float *out)
+{
+    if (!c || !in || !out) return fail(c, CZ_E_ARG, "NULL argument");
+    if (nbytes < kMaskBytes || nbytes > kMaxRecord + 4) return fail(c, CZ_E_CORRUPT, "record size out of range");
+    CZ_TRY(set_device(c));
+    CZ_TRY(grow(c, c->tmp_field, sizeof(float) * kBS3));
+    const size_t need = 16 + (size_t)kSlotBytes;
+    CZ_TRY(grow(c, c->tmp_in, need));
+    CZ_TRY(grow_pin(c, std::max<size_t>(4096, need)));
+    uint8_t *h = reinterpret_cast<uint8_t *>(c->pin);
+    long long off[2] = {16, 16 + 4 + (long long)nbytes};
+    memcpy(h, off, 16);
+    memcpy(h + 16, &nbytes, 4);
+    memcpy(h + 20, in, nbytes);
+    CZ_CUDA(c, cudaMemcpy(c->tmp_in.p, h, 20 + nbytes, cudaMemcpyHostToDevice));
+    cz_params p = {0.f, wtype, 0, shuffle, CZ_ENCODER_NONE, 1};
+    // offsets live at the start of tmp_in, the chunk right after them
+    CZ_TRY(cz_field_decompress(c, P<uint8_t>(c->tmp_in), P<long long>(c->tmp_in), 1, 32, 32, 32, &p, nullptr,
+                               P<float>(c->tmp_field)));
+    CZ_CUDA(c, cudaMemcpy(out, c->tmp_field.p, sizeof(float) * kBS3, cudaMemcpyDeviceToHost));
+    return CZ_OK;
+}
+
+// ---------------------------------------------------------------- LZ4
+int cz_lz4_bound(int isize) { return isize < 0 ? 0 : isize + isize / 255 + 16; }
+
+int cz_lz4_compress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out)
+{
+    if (!c || (!src && isize) || !dst || !out || isize < 0) return fail(c, CZ_E_ARG, "bad LZ4 arguments");
+    CZ_TRY(set_device(c));
+    const long long bound = lz4_bound_ll(isize);
+    const size_t in_bytes = (size_t)isize + 64;
+    CZ_TRY(grow(c, c->tmp_in, in_bytes + 64 + (size_t)bound + 64));
+    CZ_TRY(grow_pin(c, 4096));
+    uint8_t *d = P<uint8_t>(c->tmp_in);
+    const size_t meta = in_bytes + 64 - (in_bytes + 64) % 16;  // 16-aligned area after the input
+    uint8_t *dout = d + meta + 64;
+    long long *h = reinterpret_cast<long long *>(c->pin);
+    h[0] = 0;                 // in_off
+    h[1] = 0;                 // out_off
+    reinterpret_cast<int *>(h + 2)[0] = isize;
+    if (isize) CZ_CUDA(c, cudaMemcpy(d, src, isize, cudaMemcpyHostToDevice));
+    CZ_CUDA(c, cudaMemcpy(d + meta, h, 24, cudaMemcpyHostToDevice));
+    long long *doff = reinterpret_cast<long long *>(d + meta);
+    int *dlen = reinterpret_cast<int *>(d + meta + 16);
+    int *dout_len = reinterpret_cast<int *>(d + meta + 20);
+    CZ_CUDA(c, cz_launch_lz4_encode(d, doff, dlen, 1, dout, doff + 1, dout_len, 1, nullptr));
+    int n = 0;
+    CZ_CUDA(c, cudaMemcpy(&n, dout_len, 4, cudaMemcpyDeviceToHost));
+    if (n < 0) return fail(c, CZ_E_CUDA, "LZ4 encoder output exceeded its bound");
+    if (n > cap) return fail(c, CZ_E_SPACE, "LZ4 output buffer too small");
+    CZ_CUDA(c, cudaMemcpy(dst, dout, n, cudaMemcpyDeviceToHost));
+    *out = n;
+    return CZ_OK;
+}
+
+int cz_lz4_decompress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out)
+{
+    if (!c || (!src && isize) || !dst || !out || isize < 0 || cap < 0) return fail(c, CZ_E_ARG, "bad LZ4 arguments");
+    CZ_TRY(set_device(c));
+    const size_t in_bytes = ((size_t)isize + 64 + 15) / 16 * 16;
+    CZ_TRY(grow(c, c->tmp_in, in_bytes + 64 + (size_t)cap + 64));
+    CZ_TRY(grow_pin(c, 4096));
+    uint8_t *d = P<uint8_t>(c->tmp_in);
+    uint8_t *meta = d + in_bytes;
+    uint8_t *dout = meta + 64;
+    long long *h = reinterpret_cast<long long *>(c->pin);
+    h[0] = 0;
+    h[1] = 0;
+    reinterpret_cast<int *>(h + 2)[0] = isize;
+    reinterpret_cast<int *>(h + 2)[1] = cap;
+    if (isize) CZ_CUDA(c, cudaMemcpy(d, src, isize, cudaMemcpyHostToDevice));
+    CZ_CUDA(c, cudaMemcpy(meta, h, 24, cudaMemcpyHostToDevice));
+    long long *doff = reinterpret_cast<long long *>(meta);
+    int *dlen = reinterpret_cast<int *>(meta + 16);
+    int *dcap = reinterpret_cast<int *>(meta + 20);
+    int *dres = reinterpret_cast<int *>(meta + 24);
+    CZ_CUDA(c, cz_launch_lz4_decode(d, doff, dlen, 1, dout, doff + 1, dcap, dres, 1, nullptr));
+    int n = 0;
+    CZ_CUDA(c, cudaMemcpy(&n, dres, 4, cudaMemcpyDeviceToHost));
+    *out = n;
+    if (n < 0) return fail(c, CZ_E_CORRUPT, "malformed LZ4 input");
+    if (n) CZ_CUDA(c, cudaMemcpy(dst, dout, n, cudaMemcpyDeviceToHost));
+    return CZ_OK;
+}
+
+// ---------------------------------------------------------------- .cz images
+long long cz_file_bytes(cz_ctx *c, const cz_stream *s, int nx, int ny, int nz, const cz_params *p)
+{
+    if (!s || !p || check_dims(c, nx, ny, nz) != CZ_OK) return -1;
+    const std::string hdr = czf::header_text(nx / 32, ny / 32, nz / 32, p->eps, p->wtype, p->encoder);
+    return czf::image_bytes(s->data_bytes, s->nchunks, s->nblocks, hdr);
+}
+
+int cz_file_image(cz_ctx *c, const cz_stream *s, int nx, int ny, int nz, const cz_params *p, uint8_t *out,
+                  long long cap, long long *written)
+{
+    if (!c || !s || !p || !out || !written) return fail(c, CZ_E_ARG, "NULL argument");
+    CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(set_device(c));
+    const int bx = nx / 32, by = ny / 32, bz = nz / 32;
+    const long long nblocks = (long long)bx * by * bz;
+    if (s->nblocks != nblocks) return fail(c, CZ_E_ARG, "stream does not match the field extents");
+    const std::string hdr = czf::header_text(bx, by, bz, p->eps, p->wtype, p->encoder);
+    const long long need = czf::image_bytes(s->data_bytes, s->nchunks, nblocks, hdr);
+    if (need > cap) return fail(c, CZ_E_SPACE, "image buffer too small");
+    std::vector<long long> off(s->nchunks + 1);
+    CZ_CUDA(c, cudaMemcpy(off.data(), s->chunk_offsets, sizeof(long long) * (s->nchunks + 1), cudaMemcpyDeviceToHost));
+    const long long base = off[0];
+    for (auto &o : off) o -= base;
+    // payloads land directly in the caller's buffer behind the mini header
+    uint8_t *payload = out + czf::mini_header_bytes();
+    CZ_CUDA(c, cudaMemcpy(payload, s->data + base, (size_t)off[s->nchunks], cudaMemcpyDeviceToHost));
+    const int bpc = std::max(1, (int)((nblocks + s->nchunks - 1) / s->nchunks));
+    std::vector<int> bc(nblocks), bs(nblocks);
+    for (long long g = 0; g < nblocks; ++g) {
+        bc[g] = (int)(g / bpc);
+        bs[g] = (int)(g % bpc);
+    }
+    *written = czf::write_image(out, payload, off[s->nchunks], off.data(), s->nchunks, bc.data(), bs.data(), bx, by,
+                                bz, hdr);
+    return CZ_OK;
+}
+
+int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz, const cz_params *p, void *stream,
+                         uint8_t *out, long long cap, long long *written)
+{
+    if (!c || !h_field || !out || !written) return fail(c, CZ_E_ARG, "NULL argument");
+    CZ_TRY(check_params(c, p));
+    CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(set_device(c));
+    const size_t bytes = sizeof(float) * (size_t)nx * ny * nz;
+    CZ_TRY(grow(c, c->tmp_field, bytes));
+    CZ_CUDA(c, cudaMemcpyAsync(c->tmp_field.p, h_field, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    cz_stream s;
+    CZ_TRY(cz_field_compress(c, P<float>(c->tmp_field), nx, ny, nz, p, stream, &s));
+    return cz_file_image(c, &s, nx, ny, nz, p, out, cap, written);
+}
+
+int cz_image_info(const uint8_t *img, long long size, int *dims, int *encoder)
+{
+    if (!img || !dims) return CZ_E_ARG;
+    czf::Parsed ps;
+    std::string err;
+    if (czf::parse_image(img, size, ps, err) != 0) return CZ_E_CORRUPT;
+    dims[0] = ps.bx * 32;
+    dims[1] = ps.by * 32;
+    dims[2] = ps.bz * 32;
+    if (encoder) *encoder = ps.encoder;
+    return CZ_OK;
+}
+
+int cz_decompress_image(cz_ctx *c, const uint8_t *img, long long size, int wtype, int shuffle, void *stream,
+                        float *h_field, long long field_cap)
+{
+    if (!c || !img || !h_field) return fail(c, CZ_E_ARG, "NULL argument");
+    czf::Parsed ps;
+    std::string err;
+    if (czf::parse_image(img, size, ps, err) != 0) return fail(c, CZ_E_CORRUPT, err);
+    if (ps.wavelets != czf::wavelet_name(wtype))
+        return fail(c, CZ_E_ARG, "file wavelets " + ps.wavelets + " do not match wtype " + std::to_string(wtype));
+    if (ps.encoder != CZ_ENCODER_NONE && ps.encoder != CZ_ENCODER_LZ4)
+        return fail(c, CZ_E_ARG, "unsupported encoder in file");
+    const int nx = ps.bx * 32, ny = ps.by * 32, nz = ps.bz * 32;
+    const long long nelem = (long long)nx * ny * nz;
+    if (field_cap < nelem) return fail(c, CZ_E_SPACE, "output field too small");
+    CZ_TRY(set_device(c));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nchunks = (int)ps.chunk_start.size();
+    const long long nblocks = (long long)ps.bx * ps.by * ps.bz;
+    // payloads back to back on the device with a compact offset table;
+    // files from several ranks carry each rank's LUT between their chunks,
+    // those chunks are compacted on the host first
+    bool contiguous = true;
+    long long total = 0;
+    for (int i = 0; i < nchunks; ++i) {
+        if (i + 1 < nchunks && ps.chunk_start[i] + ps.chunk_size[i] != ps.chunk_start[i + 1]) contiguous = false;
+        total += ps.chunk_size[i];
+    }
+    std::vector<long long> off(nchunks + 1);
+    for (int i = 0, acc = 0; i < nchunks; ++i) {
+        off[i] = contiguous ? ps.chunk_start[i] - ps.chunk_start[0] : acc;
+        acc += (int)ps.chunk_size[i];
+    }
+    off[nchunks] = total;
+    for (int i = 0; i < nchunks; ++i)
+        if (ps.encoder == CZ_ENCODER_NONE && (off[i] % 4) != 0)
+            return fail(c, CZ_E_CORRUPT, "raw chunk payloads are not 4-byte aligned");
+    const size_t data_pad = ((size_t)total + 255) / 256 * 256;
+    CZ_TRY(grow(c, c->tmp_in, data_pad + sizeof(long long) * (nchunks + 1)));
+    CZ_TRY(grow(c, c->tmp_field, sizeof(float) * (size_t)nelem));
+    uint8_t *d = P<uint8_t>(c->tmp_in);
+    long long *doff = reinterpret_cast<long long *>(d + data_pad);
+    if (contiguous) {
+        CZ_CUDA(c, cudaMemcpyAsync(d, img + ps.chunk_start[0], (size_t)total, cudaMemcpyHostToDevice, st));
+    } else {
+        std::vector<uint8_t> packed((size_t)total);
+        for (int i = 0; i < nchunks; ++i) memcpy(&packed[off[i]], img + ps.chunk_start[i], ps.chunk_size[i]);
+        CZ_CUDA(c, cudaMemcpy(d, packed.data(), (size_t)total, cudaMemcpyHostToDevice));
+    }
+    CZ_CUDA(c, cudaMemcpyAsync(doff, off.data(), sizeof(long long) * (nchunks + 1), cudaMemcpyHostToDevice, st));
+    CZ_CUDA(c, cudaStreamSynchronize(st));
+    std::vector<CzField> f(1);
+    f[0] = CzField{P<float>(c->tmp_field), nx, ny, nz, 0.f, 0};
+    CZ_TRY(decompress_fields(c, f, nblocks, d, doff, nchunks, ps.encoder, wtype, shuffle, 1, ps.block_chunk.data(),
+                             ps.block_subid.data(), std::max(1, ps.max_subid), st));
+    CZ_CUDA(c, cudaMemcpy(h_field, c->tmp_field.p, sizeof(float) * (size_t)nelem, cudaMemcpyDeviceToHost));
+    return CZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+// cz_codec.h -- internal interface between the C-ABI layer and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+// One field of a (possibly batched) launch, x fastest [nz][ny][nx], all
+// extents multiples of 32. block0 is the global index of the field's first
+// block; blocks of a field are numbered ix fastest, then iy, iz (the
+// reference grid's order, Grid.h:81-90).
+struct CzField {
+    const float *data;
+    int nx, ny, nz;
+    float eps;
+    long long block0;
+};
+
+extern "C" int cz_codec_smem_bytes(void);
+
+cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long long total_blocks, int zerobits,
+                             int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
+                             cudaStream_t st);
+// Record of block g at base + rec_off[g] ([int32 nbytes][record]); a
+// negative rec_off marks a block whose record is missing (status -1).
+cudaError_t cz_launch_decode(int wtype, const CzField *fields, int nfields, long long total_blocks, int shuffle,
+                             const uint8_t *base, const long long *rec_off, int *status, unsigned long long *queue,
+                             int grid, cudaStream_t st);
+
+// LZ4 stage (cz_lz4.cu). Chunk c's input is in[in_off[c] .. in_off[c]+in_len[c]).
+cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
+                                 uint8_t *out, const long long *out_off, int *out_len, int grid, cudaStream_t st);
+cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
+                                 uint8_t *out, const long long *out_off, const int *out_cap, int *out_len, int grid,
+                                 cudaStream_t st);
+
+// Stream assembly helpers (cz_lz4.cu, cz_stream.cu)
+cudaError_t cz_launch_gather(const uint8_t *src, const long long *src_off, const int *len, int nchunks,
+                             uint8_t *dst, const long long *dst_off, cudaStream_t st);
+// Chunk layout of the encode side: chunk c holds blocks [c*bpc, (c+1)*bpc).
+// Fills in_off/in_len (chunk inputs in chunk_in, or in the slots when bpc=1),
+// blk_dst (where block g's [nbytes][record] goes inside chunk_in) and lz_off.
+cudaError_t cz_launch_chunk_setup(int bpc, long long nblocks, int nchunks, const int *rec_bytes, long long *in_off,
+                                  int *in_len, long long *blk_dst, long long *lz_off, long long lz_slot,
+                                  cudaStream_t st);
+// Copies block g's [nbytes][record] from its slot to chunk_in + blk_dst[g].
+cudaError_t cz_launch_pack_records(const uint8_t *stage, const int *rec_bytes, long long nblocks,
+                                   const long long *blk_dst, uint8_t *chunk_in, cudaStream_t st);
+// Exclusive scan of len[0..n) into off[0..n], off[n] = total (n <= 2^31).
+cudaError_t cz_launch_scan(const int *len, int n, long long *off, cudaStream_t st);
+// Decode side: walks the [nbytes] headers of each decoded chunk (chunk c at
+// base + c*chunk_cap, dec_len[c] bytes) and records where every block's
+// record starts (rec_off, relative to base); -1 and status -1 on a short or
+// malformed chunk. src_off/src_len, if not NULL, give raw (not LZ4) chunks.
+cudaError_t cz_launch_locate_records(int bpc, long long nblocks, int nchunks, const long long *chunk_base,
+                                     const int *dec_len, long long *rec_off, int *status, const uint8_t *base,
+                                     cudaStream_t st);
+cudaError_t cz_launch_decode_setup(int nchunks, const long long *off, int *in_len, long long *dec_off, int *dec_cap,
+                                   long long cap, int raw, cudaStream_t st);
+cudaError_t cz_launch_chunk_records(int nchunks, int maxsub, const long long *chunk_base, const int *dec_len,
+                                    const uint8_t *base, long long *chunk_rec, cudaStream_t st);
+cudaError_t cz_launch_map_blocks(long long nblocks, int nchunks, int maxsub, const int *block_chunk,
+                                 const int *block_subid, const long long *chunk_rec, long long *rec_off,
+                                 cudaStream_t st);
+cudaError_t cz_launch_status_reduce(const int *status, long long n, int *flag, cudaStream_t st);
+cudaError_t cz_launch_neg_reduce(const int *v, int n, int *flag, cudaStream_t st);
+cudaError_t cz_launch_rebase(long long *off, int n, long long base, cudaStream_t st);

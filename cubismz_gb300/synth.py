@@ -31,36 +31,43 @@ def _noise(shape, rng, rms):
     return f * (rms / s) if s > 0 else f
 
 
+def _box(c, r, n):
+    return max(0, int(np.floor(c - r))), min(n, int(np.ceil(c + r)) + 1)
+
+
 def generate(shape, seed=0, blobs=20, interfaces=3, noise_rms=0.05, mean=1.0, velocity=False):
     """One field of the given (nz, ny, nx) shape.
 
-    blobs: Gaussian blobs with amplitude U[0.5,2] and sigma U[4,16] cells;
-    interfaces: tanh spheres of width 2 cells and jump 1.0;
+    blobs: Gaussian blobs with amplitude U[0.5,2] and sigma U[4,16] cells,
+    evaluated within 8 sigma of their centre (beyond it they are below
+    1e-13 of their amplitude);
+    interfaces: tanh spheres of width 2 cells and jump 1.0, evaluated within
+    a box reaching 40 cells beyond the sphere (farther out the profile is
+    below 1e-17);
     velocity=True: random signs on the blob amplitudes, then zero mean and
     unit rms; otherwise the field is offset to `mean`.
     """
     nz, ny, nx = shape
     rng = np.random.default_rng(seed)
-    z = np.arange(nz, dtype=np.float64)[:, None, None]
-    y = np.arange(ny, dtype=np.float64)[None, :, None]
-    x = np.arange(nx, dtype=np.float64)[None, None, :]
     f = np.zeros(shape, np.float64)
     for _ in range(blobs):
         a = rng.uniform(0.5, 2.0) * (rng.choice([-1.0, 1.0]) if velocity else 1.0)
         sig = rng.uniform(4.0, 16.0)
         cz, cy, cx = rng.uniform(0, nz), rng.uniform(0, ny), rng.uniform(0, nx)
-        # separable evaluation keeps memory at one field
-        gz = np.exp(-((z - cz) ** 2) / (2 * sig * sig))
-        gy = np.exp(-((y - cy) ** 2) / (2 * sig * sig))
-        gx = np.exp(-((x - cx) ** 2) / (2 * sig * sig))
-        f += a * (gz * gy) * gx
+        (z0, z1), (y0, y1), (x0, x1) = _box(cz, 8 * sig, nz), _box(cy, 8 * sig, ny), _box(cx, 8 * sig, nx)
+        gz = np.exp(-((np.arange(z0, z1) - cz) ** 2) / (2 * sig * sig))[:, None, None]
+        gy = np.exp(-((np.arange(y0, y1) - cy) ** 2) / (2 * sig * sig))[None, :, None]
+        gx = np.exp(-((np.arange(x0, x1) - cx) ** 2) / (2 * sig * sig))[None, None, :]
+        f[z0:z1, y0:y1, x0:x1] += a * (gz * gy) * gx
     f += _noise(shape, rng, noise_rms)
     lo = min(nx, ny, nz)
     for _ in range(interfaces):
         cz, cy, cx = rng.uniform(0, nz), rng.uniform(0, ny), rng.uniform(0, nx)
         r0 = rng.uniform(0.1, 0.3) * lo
-        r = np.sqrt((z - cz) ** 2 + (y - cy) ** 2 + (x - cx) ** 2)
-        f += 0.5 * (1.0 - np.tanh((r - r0) / 2.0))
+        (z0, z1), (y0, y1), (x0, x1) = _box(cz, r0 + 40, nz), _box(cy, r0 + 40, ny), _box(cx, r0 + 40, nx)
+        r = np.sqrt((np.arange(z0, z1)[:, None, None] - cz) ** 2 + (np.arange(y0, y1)[None, :, None] - cy) ** 2 +
+                    (np.arange(x0, x1)[None, None, :] - cx) ** 2)
+        f[z0:z1, y0:y1, x0:x1] += 0.5 * (1.0 - np.tanh((r - r0) / 2.0))
     if velocity:
         f -= f.mean()
         s = f.std()

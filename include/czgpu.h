@@ -1,0 +1,166 @@
+/*
+ * czgpu.h -- C-ABI of the GB300 wavelet compression path (libczgpu.so).
+ *
+ * Drop-in for the per-block codec and lossless stage of CubismZ
+ * (fab4100/CubismZ). Plain C types only; every entry point returns an int
+ * status (CZ_OK or a negative CZ_E* code) and never aborts. Device pointers
+ * are CUDA global memory of the context's device; `stream` is a
+ * cudaStream_t passed as void* (NULL = legacy default stream).
+ *
+ * Reference interfaces replaced (paths within the reference project):
+ *   WaveletCompressorGeneric<32,float>::compress / decompress
+ *       Compressor/source/WaveletCompressor.h:61-71, WaveletCompressor.cpp:152-259
+ *   deflate_inplace (LZ4 branch) / zdecompress
+ *       Compressor/source/CompressionEncoders.h:45-46, 113-247, 48-88
+ *   LZ4_compress / LZ4_uncompress_unknownOutputSize
+ *       ThirdParty/lz4/lz4.h:53,112 (lz4.c:695-700, 802-905)
+ *   the writer's block loop and .cz layout
+ *       Compressor/source/SerializerIO_WaveletCompression_MPI_Simple.h:187-345, 347-466, 489-644
+ *   the reader's load_file / load_block2
+ *       Compressor/source/Reader_WaveletCompression.h:255-560, 635-754
+ */
+#ifndef CZGPU_H
+#define CZGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CZ_OK 0
+#define CZ_E_ARG -1      /* invalid argument (sizes, pointers, parameters) */
+#define CZ_E_CUDA -2     /* a CUDA call failed */
+#define CZ_E_CORRUPT -3  /* malformed record, LZ4 stream or .cz file */
+#define CZ_E_SPACE -4    /* caller buffer too small */
+#define CZ_E_NOMEM -5    /* device or host allocation failed */
+
+#define CZ_BLOCKSIZE 32
+#define CZ_BLOCK_ELEMS 32768
+#define CZ_MASK_BYTES 4096
+#define CZ_MAX_RECORD (4096 + 4 * 32768) /* WaveletCompressor.h:40-45 */
+
+#define CZ_ENCODER_NONE 0 /* "Encoder: none"  (CompressionEncoders.h:240-246) */
+#define CZ_ENCODER_LZ4 1  /* "Encoder: lz4"   (CompressionEncoders.h:192-238) */
+
+typedef struct cz_ctx cz_ctx;
+
+/* Codec parameters: the reference's compile-time switches as run-time values.
+ *   eps        absolute threshold, |c| > eps is kept (FullWaveletTransform.h:84)
+ *   wtype      1 interp 4th order, 2 lifted interp, 3 average-interp 3rd order
+ *              (any other value behaves as 3, WaveletsOnInterval.h:154)
+ *   zerobits   0 or n: clear the n low bits of every survivor (-D_ZEROBITS_=n)
+ *   shuffle    0/1: byte-plane shuffle of the survivors (-D_USE_SHUFFLE3_)
+ *   encoder    CZ_ENCODER_NONE or CZ_ENCODER_LZ4
+ *   blocks_per_chunk  records per lossless chunk (1 is the default) */
+typedef struct {
+    float eps;
+    int wtype;
+    int zerobits;
+    int shuffle;
+    int encoder;
+    int blocks_per_chunk;
+} cz_params;
+
+/* Compressed field held in device memory owned by the context (valid until
+ * the next call on the context). data: chunk payloads back to back;
+ * chunk_offsets[nchunks+1]: offsets into data; block_chunk/block_subid: the
+ * chunk and index within the chunk of every block (BlockMetadata fields);
+ * raw_bytes: total record bytes before the lossless stage. */
+typedef struct {
+    const uint8_t *data;
+    long long data_bytes;
+    const long long *chunk_offsets; /* device */
+    int nchunks;
+    long long nblocks;
+    long long raw_bytes;
+} cz_stream;
+
+/* ---- context ---------------------------------------------------------- */
+/* New context on `device` (scratch buffers are allocated on first use and
+ * grown as needed). */
+int cz_create(int device, cz_ctx **out);
+int cz_destroy(cz_ctx *ctx);
+/* Last error text of the context (never NULL). */
+const char *cz_last_error(cz_ctx *ctx);
+
+/* Per-stage device timing (CUDA events on the call's stream), the
+ * counterpart of the writer's fwt/encoding timers
+ * (SerializerIO_WaveletCompression_MPI_Simple.h:201-203, 325, 341-343).
+ * After cz_set_timing(ctx, 1), every field call records its stages;
+ * cz_stage_times writes up to n durations in milliseconds:
+ *   compress:   [0] codec kernel, [1] lossless stage, [2] stream assembly
+ *   decompress: [0] lossless stage, [1] record location, [2] codec kernel
+ * and returns how many were written. */
+int cz_set_timing(cz_ctx *ctx, int on);
+int cz_stage_times(cz_ctx *ctx, float *ms, int n);
+
+/* ---- per-block drop-in (host buffers) --------------------------------- */
+/* WaveletCompressor::compress of one 32^3 block in[z][y][x]: writes the
+ * record [4096-byte mask][survivors] to out (capacity CZ_MAX_RECORD) and its
+ * size to *nbytes. Replaces WaveletCompressor.cpp:152-182. */
+int cz_block_compress(cz_ctx *ctx, const float *in, float eps, int wtype, int zerobits, int shuffle, uint8_t *out,
+                      int *nbytes);
+/* WaveletCompressor::decompress of one record into out[z][y][x].
+ * Replaces WaveletCompressor.cpp:231-259 (+ copy_to, WaveletCompressor.h:66-82). */
+int cz_block_decompress(cz_ctx *ctx, const uint8_t *in, int nbytes, int wtype, int shuffle, float *out);
+
+/* ---- LZ4 pair (host buffers) ------------------------------------------ */
+/* Worst-case output size, LZ4_compressBound (lz4.h:81-82). */
+int cz_lz4_bound(int isize);
+/* Compress src[0..isize) into dst (capacity cap >= cz_lz4_bound(isize));
+ * *out = compressed size. Replaces LZ4_compress (lz4.c:695-700). */
+int cz_lz4_compress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out);
+/* Decode with the acceptance rules of LZ4_uncompress_unknownOutputSize
+ * (lz4.c:802-905); *out = decoded size. Malformed input -> CZ_E_CORRUPT. */
+int cz_lz4_decompress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out);
+
+/* ---- field level (device buffers) ------------------------------------- */
+/* Compress a field d_field[nz][ny][nx] (extents multiples of 32) into the
+ * context's stream buffers. Asynchronous on `stream` except that it waits
+ * for the stream's compressed size. Replaces the writer's _compress loop
+ * (SerializerIO...:187-345) for one rank. */
+int cz_field_compress(cz_ctx *ctx, const float *d_field, int nx, int ny, int nz, const cz_params *p, void *stream,
+                      cz_stream *out);
+/* Copy a compressed stream into caller-owned device buffers: d_data
+ * (s->data_bytes bytes) and d_chunk_offsets (s->nchunks+1 entries, rebased
+ * to start at 0). Either pointer may be NULL. */
+int cz_stream_copy(cz_ctx *ctx, const cz_stream *s, uint8_t *d_data, long long *d_chunk_offsets, void *stream);
+/* Decompress chunks (d_data, d_chunk_offsets[nchunks+1], device) holding
+ * the records of the field's blocks in block order, blocks_per_chunk per
+ * chunk, into d_field. */
+int cz_field_decompress(cz_ctx *ctx, const uint8_t *d_data, const long long *d_chunk_offsets, int nchunks, int nx,
+                        int ny, int nz, const cz_params *p, void *stream, float *d_field);
+
+/* Many fields of uneven extents and thresholds in one persistent launch
+ * (device work queue). eps[i] per field; p->eps is ignored. out[i]
+ * describes field i's chunks inside the shared stream buffers. */
+int cz_batch_compress(cz_ctx *ctx, int nfields, const float *const *d_fields, const int *dims /* 3*nfields: nx,ny,nz */,
+                      const float *eps, const cz_params *p, void *stream, cz_stream *out);
+
+/* ---- .cz files (host memory) ------------------------------------------ */
+/* Size of the .cz image for a compressed stream (header, metadata, LUT). */
+long long cz_file_bytes(cz_ctx *ctx, const cz_stream *s, int nx, int ny, int nz, const cz_params *p);
+/* Write the .cz image of `s` into host buffer out (capacity cap): the
+ * reference writer's layout (SerializerIO...:347-466, 489-591) for one rank.
+ * *written = image size. */
+int cz_file_image(cz_ctx *ctx, const cz_stream *s, int nx, int ny, int nz, const cz_params *p, uint8_t *out,
+                  long long cap, long long *written);
+/* Host field in, .cz image out: H2D copy, compression, D2H copy and layout
+ * in one call (the end-to-end drop-in for Write<channel>). */
+int cz_compress_to_image(cz_ctx *ctx, const float *h_field, int nx, int ny, int nz, const cz_params *p,
+                         void *stream, uint8_t *out, long long cap, long long *written);
+/* Parse a .cz image: dims[3] (nx,ny,nz) and the encoder it declares. */
+int cz_image_info(const uint8_t *img, long long size, int *dims, int *encoder);
+/* .cz image in, host field out (the reader's load_file + load_block2 for
+ * every block, Reader_WaveletCompression.h:255-754). wtype must match the
+ * file's "Wavelets:" entry; shuffle is the build option the file was
+ * written with (the format does not record it). */
+int cz_decompress_image(cz_ctx *ctx, const uint8_t *img, long long size, int wtype, int shuffle, void *stream,
+                        float *h_field, long long field_cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -95,7 +95,7 @@ def block_compress(block, eps, wtype, zerobits=0, shuffle=0):
 
 def block_decompress(record, wtype, shuffle=0):
     r = np.ascontiguousarray(record, dtype=np.uint8)
-    out = np.zeros(BS3, np.float32)
+    out = np.zeros((32, 32, 32), np.float32)
     rc = lib().czo_block_decompress(_p(r, _u8p), r.size, wtype, shuffle, _p(out, _fp))
     if rc != 0:
         raise ValueError(f"oracle rejected the record ({rc})")
@@ -193,7 +193,7 @@ def ref_block_compress(L, block, eps, wtype):
 def ref_block_decompress(L, record, wtype):
     r = np.zeros(MAXRECORD + 16, np.uint8)
     r[: len(record)] = record
-    out = np.zeros(BS3, np.float32)
+    out = np.zeros((32, 32, 32), np.float32)
     L.ref_block_decompress(_p(r, _u8p), len(record), wtype, _p(out, _fp))
     return out
 

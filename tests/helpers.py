@@ -1,0 +1,81 @@
+"""Helpers shared by the tests (fixtures, block iteration, the RES line)."""
+import hashlib
+import zlib
+
+import numpy as np
+
+
+def sha(b):
+    return hashlib.sha256(bytes(b)).hexdigest()
+
+
+def blocks(field):
+    nz, ny, nx = field.shape
+    for bz in range(nz // 32):
+        for by in range(ny // 32):
+            for bx in range(nx // 32):
+                yield field[bz * 32:bz * 32 + 32, by * 32:by * 32 + 32, bx * 32:bx * 32 + 32].copy()
+
+
+def seeded_blocks():
+    """The blocks make_golden.py hashed the reference outputs of."""
+    from cubismz_gb300 import synth
+    rng = np.random.default_rng(2024)
+    small = synth.config_field("small", 0)
+    out = [small[:32, :32, :32].copy(), small[32:64, 64:96, 96:128].copy()]
+    out.append((rng.standard_normal(32 ** 3) * 1e-3 + 1.0).astype(np.float32).reshape(32, 32, 32))
+    out.append((rng.standard_normal(32 ** 3) * 10.0 ** rng.uniform(-6, 6, 32 ** 3)).astype(np.float32)
+               .reshape(32, 32, 32))
+    return out
+
+
+def res_line(orig, dec, fsize):
+    """cz2diff's RES line (Tools/cz2diff.cpp:116-261): CR, relative and mean
+    errors, bits per sample and PSNR = 20 log10((max-min)/(2 sqrt(MSE)))."""
+    f1 = dec.astype(np.float64).ravel()
+    f2 = orig.astype(np.float64).ravel()
+    err = np.abs(f1 - f2)
+    n = f1.size
+    e_inf, n_inf = err.max(), np.abs(f2).max()
+    e1, n1 = err.sum(), np.abs(f2).sum()
+    e2, n2 = (err * err).sum(), (f2 * f2).sum()
+    mse = e2 / n
+    psnr = 20 * np.log10((f2.max() - f2.min()) / (2 * np.sqrt(mse)))
+    return "RES: %12.2f %.6e %.6e %.6e %.6e %.6e %12.04f %12.04f" % (
+        4.0 * n / fsize, e_inf / n_inf, e1 / n1, e1 / n, np.sqrt(e2) / np.sqrt(n2), np.sqrt(e2) / n,
+        fsize * 8.0 / n, psnr)
+
+
+def header_text(bx, by, bz, threshold, wavelets, encoder):
+    """The .cz ASCII header (SerializerIO_WaveletCompression_MPI_Simple.h:495-556)."""
+    mx = max(bx, by, bz)
+    h = (1.0 / mx) / 32
+
+    def g(v):  # iostream default formatting: %g, precision 6
+        return "%g" % v
+
+    return ("\n==============START-ASCI-HEADER==============\n"
+            "Endianess: little\nsizeofReal: 4\nsizeofsize_t: 8\nsizeofBlockMetadata: 20\n"
+            "sizeofHeaderLUT: 12\nsizeofCompressedBlock: 20\nBlocksize: 32\n"
+            f"Blocks: {bx} x {by} x {bz}\nExtent: {g(h * bx * 32)} {g(h * by * 32)} {g(h * bz * 32)}\n"
+            f"SubdomainBlocks: {bx} x {by} x {bz}\nHalfFloat: no\nWavelets: {wavelets}\n"
+            f"WaveletThreshold: {g(float(np.float32(threshold)))}\nEncoder: {encoder}\n"
+            "==============START-BINARY-METABLOCKS==============\n")
+
+
+OCEAN = "\n==============START-BINARY-OCEAN==============\n"
+LUTTITLE = "\n==============START-BINARY-LUT==============\n"
+
+
+def cz_size(chunk_sizes, nblocks, header):
+    return 8 + len(OCEAN) + sum(chunk_sizes) + 8 * len(chunk_sizes) + len(header) + 20 * nblocks + len(LUTTITLE) + 12
+
+
+def zlib_chunks(raw, off, bpc, nblocks):
+    """Regroup one-record chunks into bpc-record chunks and deflate each with
+    zlib's default level, as deflate_inplace does (CompressionEncoders.h:116-190)."""
+    out = []
+    for c0 in range(0, nblocks, bpc):
+        c1 = min(nblocks, c0 + bpc)
+        out.append(zlib.compress(bytes(raw[off[c0]:off[c1]]), 6))
+    return out

@@ -1,0 +1,68 @@
+"""GPU LZ4 stage: reference-encoded streams decode with the GPU decoder;
+GPU-encoded streams decode with the restated reference decoder (and the
+reference's own, where it was built); malformed input is rejected without
+faulting."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import czoracle as O
+from tests.helpers import sha
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cz(gpu_lib):
+    import cubismz_gb300 as cz
+    return cz
+
+
+def test_gpu_decodes_reference_lz4(cz, golden):
+    data = open(os.path.join(os.path.dirname(__file__), "golden", "ref_lz4_chunks.bin"), "rb").read()
+    pos = 0
+    for entry in golden["ref_lz4_chunks"]:
+        zn, rn = np.frombuffer(data[pos:pos + 8], np.int32)
+        z = data[pos + 8:pos + 8 + zn]
+        pos += 8 + zn
+        out = cz.lz4_decompress(z, int(rn))
+        assert len(out) == entry["raw_bytes"] and sha(out) == entry["raw_sha256"]
+
+
+def test_gpu_lz4_roundtrip(cz, small_field):
+    rng = np.random.default_rng(9)
+    raw, off = O.field_compress(small_field, 1e-3, 1, 4, 1, 0, 1)
+    samples = [b"", b"x", bytes(12), bytes(13), bytes(70000), rng.integers(0, 256, 100000, np.uint8).tobytes(),
+               (b"0123456789abcdef" * 5000), bytes(raw[off[0]:off[1]]), bytes(raw[off[7]:off[9]])]
+    L = O.ref(4, 1, "lz4")
+    for d in samples:
+        z = cz.lz4_compress(d)
+        assert len(z) <= len(d) + len(d) // 255 + 16
+        n, out = O.lz4_decompress(z, len(d))
+        assert n == len(d) and out.tobytes() == d
+        assert cz.lz4_decompress(z, len(d)) == d
+        if L is not None:
+            n2, out2 = O.ref_lz4_decompress(L, z, len(d))
+            assert n2 == len(d) and out2.tobytes() == d
+
+
+def test_gpu_lz4_rejects_malformed(cz):
+    d = bytes(4000) + b"pattern!" * 500
+    z = cz.lz4_compress(d)
+    with pytest.raises(cz.CzError):
+        cz.lz4_decompress(z, 100)  # output too small
+    bad = bytearray(z)
+    bad[0] = 0xF0  # literal length runs past the input
+    with pytest.raises(cz.CzError):
+        cz.lz4_decompress(bytes(bad[:3]), len(d))
+    rng = np.random.default_rng(1)
+    for _ in range(20):
+        junk = rng.integers(0, 256, int(rng.integers(1, 300)), np.uint8).tobytes()
+        try:
+            out = cz.lz4_decompress(junk, 4096)
+            n, ref = O.lz4_decompress(junk, 4096)
+            assert n == len(out) and ref.tobytes() == out
+        except cz.CzError:
+            n, _ = O.lz4_decompress(junk, 4096)
+            assert n <= 0
