@@ -73,7 +73,8 @@ int grow(cz_ctx *c, DevBuf &b, size_t bytes)
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.cap = 0;
-    size_t want = bytes < 256 ? 256 : bytes;
+    // 256 bytes of tail room: word-wise copies may read a few bytes past the end
+    size_t want = bytes + 256;
     if (cudaMalloc(&b.p, want) != cudaSuccess) {
         cudaGetLastError();
         return fail(c, CZ_E_NOMEM, "device allocation of " + std::to_string(want) + " bytes failed");
@@ -214,8 +215,8 @@ int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nbl
     if (p->encoder == CZ_ENCODER_LZ4) {
         const int lzgrid = std::max(1, std::min((nchunks + 3) / 4, c->sms * 8));
         CZ_CUDA(c, cz_launch_lz4_encode(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
-                                        P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<int>(c->lz_len), lzgrid,
-                                        st));
+                                        P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<int>(c->lz_len),
+                                        p->shuffle ? 1 : 0, lzgrid, st));
         CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len), nchunks, P<int>(c->flag), st));
         gsrc = P<uint8_t>(c->lz_out);
         gsrc_off = P<long long>(c->lz_off);
@@ -522,7 +523,7 @@ int cz_lz4_compress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int 
     long long *doff = reinterpret_cast<long long *>(d + meta);
     int *dlen = reinterpret_cast<int *>(d + meta + 16);
     int *dout_len = reinterpret_cast<int *>(d + meta + 20);
-    CZ_CUDA(c, cz_launch_lz4_encode(d, doff, dlen, 1, dout, doff + 1, dout_len, 1, nullptr));
+    CZ_CUDA(c, cz_launch_lz4_encode(d, doff, dlen, 1, dout, doff + 1, dout_len, 0, 1, nullptr));
     int n = 0;
     CZ_CUDA(c, cudaMemcpy(&n, dout_len, 4, cudaMemcpyDeviceToHost));
     if (n < 0) return fail(c, CZ_E_CUDA, "LZ4 encoder output exceeded its bound");

@@ -11,29 +11,50 @@
 //   (WaveletCompressor.cpp:231-259): deserialize_bitset, reshuffle3, load
 //   (FullWaveletTransform.h:99-150) and iwt.
 //
-// One CTA per SM, persistent; blocks are taken from a device work queue so
-// one launch serves one field or a batch of uneven fields. A block is held
-// whole in shared memory (128 KiB, swizzled); while a block is thresholded
-// and emitted, the next block's 128 KiB is already in flight into registers.
+// One CTA of 512 threads per SM, persistent; blocks come from a device work
+// queue, so one launch serves one field or a batch of uneven fields.
+//
+// Block layout in shared memory: coefficient (x,y,z) at x + 33y + 1057z. Lines
+// along any axis are read with immediate offsets and hit 32 distinct banks
+// (lane strides 33 and 1057 are 1 mod 32).
+//
+// Thresholding is fused into the last sweep of each level: the thread that
+// finishes a line holds exactly one run of the reference's survivor order
+// per octant (16 coefficients along z at level 32, 8 along y at level 16, 4
+// along x at level 8, cz_layout.cuh) and the matching bits of one mask word,
+// so it records a keep mask per run and its mask bits. One scan over the run
+// counts gives every run's output offset; one pass then writes the survivors.
+//
+// Encode pipeline per block: the x sweep takes its lines from registers that
+// were loaded while the previous block was finishing (levels 16/8, scan and
+// emission), so HBM reads overlap compute.
 #include "cz_codec.h"
 #include "cz_device.cuh"
 
 namespace cz {
 
-#ifndef CZ_CODEC_THREADS
-#define CZ_CODEC_THREADS 256
-#endif
-constexpr int kNT = CZ_CODEC_THREADS;  // threads per CTA (one CTA per SM)
+constexpr int kNT = 512;
 constexpr int kNW = kNT / 32;
-constexpr int kChunksPerWarp = 1024 / kNW;  // 32-entry survivor-order chunks
-constexpr int kPrefetch = (kBS3 / 4) / kNT;  // float4 per thread per block
+constexpr int SY = 33, SZ = 1057;
+constexpr int kPadFloats = 32 * SZ;  // 33824
+__device__ __forceinline__ int pidx(int x, int y, int z) { return x + SY * y + SZ * z; }
+
+// survivor-order runs ("segments"): coarse (64 entries, always kept), then
+// level 8 (7 codes x 16 runs of 4), level 16 (7 x 64 runs of 8), level 32
+// (7 x 256 runs of 16)
+constexpr int kSeg8 = 112, kSeg16 = 448, kSeg32 = 1792;
+constexpr int kSegBase8 = 1, kSegBase16 = kSegBase8 + kSeg8, kSegBase32 = kSegBase16 + kSeg16;
+constexpr int kSegs = kSegBase32 + kSeg32;  // 2353
 
 // shared memory map (bytes)
 constexpr int kSmBlock = 0;
-constexpr int kSmMask = kBS3 * 4;
-constexpr int kSmBallot = kSmMask + kMaskBytes;
-constexpr int kSmWarp = kSmBallot + 1024 * 4;
-constexpr int kSmBytes = kSmWarp + 64 * 4;
+constexpr int kSmMask = ((kPadFloats * 4 + 15) / 16) * 16;  // 4096 B, u32 words
+constexpr int kSmSeg32 = kSmMask + kMaskBytes;              // u16 x 1792
+constexpr int kSmSeg16 = kSmSeg32 + kSeg32 * 2;             // u8 x 448
+constexpr int kSmSeg8 = kSmSeg16 + kSeg16;                  // u8 x 112
+constexpr int kSmOff = ((kSmSeg8 + kSeg8 + 15) / 16) * 16;  // int x kSegs
+constexpr int kSmWarp = ((kSmOff + 4 * (kSegs + 1) + 15) / 16) * 16;
+constexpr int kSmBytes = kSmWarp + 4 * 64;
 
 struct BlockRef {
     const CzField *f;
@@ -59,57 +80,230 @@ __device__ __forceinline__ BlockRef locate(const CzField *fields, int nfields, l
     return r;
 }
 
-__device__ __forceinline__ const float *row_ptr(const BlockRef &r, int y, int z)
+__device__ __forceinline__ size_t row_offset(const BlockRef &r, int y, int z)
 {
     const CzField &f = *r.f;
-    return f.data + ((size_t)(r.bz * 32 + z) * f.ny + (size_t)(r.by * 32 + y)) * f.nx + r.bx * 32;
+    return ((size_t)(r.bz * 32 + z) * f.ny + (size_t)(r.by * 32 + y)) * f.nx + (size_t)r.bx * 32;
 }
 
-__device__ __forceinline__ void prefetch_block(const BlockRef &r, float4 (&pf)[kPrefetch])
+// Rows (y, z) and (y, z+16) of a block, y = tid&31, z = tid>>5: the two x
+// lines this thread transforms first.
+__device__ __forceinline__ void load_rows(const BlockRef &r, float4 (&pf)[16])
+{
+    const int y = threadIdx.x & 31, z = threadIdx.x >> 5;
+    const float4 *r0 = reinterpret_cast<const float4 *>(r.f->data + row_offset(r, y, z));
+    const float4 *r1 = reinterpret_cast<const float4 *>(r.f->data + row_offset(r, y, z + 16));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) pf[k] = __ldg(r0 + k);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) pf[8 + k] = __ldg(r1 + k);
+}
+
+template <int N>
+__device__ __forceinline__ unsigned keep_bits(const float (&v)[N], float eps)
+{
+    unsigned b = 0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) b |= (unsigned)(fabsf(v[j]) > eps) << j;  // FullWaveletTransform.h:84
+    return b;
+}
+
+// ------------------------------------------------------------------ sweeps
+// Line l of a sweep along AXIS over the [0,N)^3 corner: the two other
+// coordinates are (l % N, l / N), lowest first.
+template <int N, int AXIS>
+__device__ __forceinline__ int line_base(int l)
+{
+    const int a = l % N, c = l / N;
+    if (AXIS == 0) return pidx(0, a, c);
+    if (AXIS == 1) return pidx(a, 0, c);
+    return pidx(a, c, 0);
+}
+template <int AXIS>
+__host__ __device__ constexpr int stride() { return AXIS == 0 ? 1 : (AXIS == 1 ? SY : SZ); }
+
+template <int N, int AXIS>
+__device__ __forceinline__ void ld_line(const float *sb, int base, float (&v)[N])
 {
 #pragma unroll
-    for (int k = 0; k < kPrefetch; ++k) {
-        const int i = threadIdx.x + k * kNT;
-        const int row = i >> 3, c = i & 7;
-        pf[k] = __ldcs(reinterpret_cast<const float4 *>(row_ptr(r, row & 31, row >> 5)) + c);
+    for (int j = 0; j < N; ++j) v[j] = sb[base + j * stride<AXIS>()];
+}
+template <int N, int AXIS>
+__device__ __forceinline__ void st_line(float *sb, int base, const float (&v)[N])
+{
+#pragma unroll
+    for (int j = 0; j < N; ++j) sb[base + j * stride<AXIS>()] = v[j];
+}
+
+template <int N, int AXIS, bool FWD, int KIND>
+__device__ __forceinline__ void sweep(float *sb)
+{
+    for (int l = threadIdx.x; l < N * N; l += kNT) {
+        const int base = line_base<N, AXIS>(l);
+        float v[N];
+        ld_line<N, AXIS>(sb, base, v);
+        if (FWD) line_fwd<N, KIND>(v);
+        else line_inv<N, KIND>(v);
+        st_line<N, AXIS>(sb, base, v);
     }
 }
 
-__device__ __forceinline__ void stage_block(float *sb, const float4 (&pf)[kPrefetch])
+// ------------------------------------------------------------ thresholding
+struct Shared {
+    float *sb;
+    uint32_t *mask32;
+    uint16_t *seg32;
+    uint8_t *seg16, *seg8;
+    int *off, *warp;
+};
+
+__device__ __forceinline__ Shared carve(unsigned char *smem)
 {
-#pragma unroll
-    for (int k = 0; k < kPrefetch; ++k) {
-        const int i = threadIdx.x + k * kNT;
-        const int row = i >> 3, x0 = (i & 7) * 4;
-        const int y = row & 31, z = row >> 5;
-        sb[swz(x0 + 0, y, z)] = pf[k].x;
-        sb[swz(x0 + 1, y, z)] = pf[k].y;
-        sb[swz(x0 + 2, y, z)] = pf[k].z;
-        sb[swz(x0 + 3, y, z)] = pf[k].w;
-    }
+    Shared s;
+    s.sb = reinterpret_cast<float *>(smem + kSmBlock);
+    s.mask32 = reinterpret_cast<uint32_t *>(smem + kSmMask);
+    s.seg32 = reinterpret_cast<uint16_t *>(smem + kSmSeg32);
+    s.seg16 = smem + kSmSeg16;
+    s.seg8 = smem + kSmSeg8;
+    s.off = reinterpret_cast<int *>(smem + kSmOff);
+    s.warp = reinterpret_cast<int *>(smem + kSmWarp);
+    return s;
 }
 
-// Block-wide exclusive scan of one count per warp; returns the warp's offset
-// and the total through *total.
-__device__ __forceinline__ int warp_offsets(int *swarp, int cnt, int *total)
+// Level-32 z line (x,y): positional word y*32+x holds its bits z (px = z,
+// py = x, pz = y); runs are z<16 (octant code with px bit 0) and z>=16.
+__device__ __forceinline__ void emit32(const Shared &s, int x, int y, unsigned kb)
 {
+    const int chi = 1 | ((x >= 16) << 1) | ((y >= 16) << 2);
+    const int sub = ((y & 15) << 4) | (x & 15);
+    s.seg32[(chi - 1) * 256 + sub] = (uint16_t)(kb >> 16);
+    const int w = x + 32 * y;
+    if (chi > 1) {
+        s.seg32[(chi - 2) * 256 + sub] = (uint16_t)kb;
+        s.mask32[w] = kb;
+    } else {
+        reinterpret_cast<uint16_t *>(s.mask32)[2 * w + 1] = (uint16_t)(kb >> 16);
+    }
+}
+// Level-16 y line (x,z): positional word x*32+z holds its bits y (px = y,
+// py = z, pz = x); runs are y<8 and y>=8.
+__device__ __forceinline__ void emit16(const Shared &s, int x, int z, unsigned kb)
+{
+    const int chi = 1 | ((z >= 8) << 1) | ((x >= 8) << 2);
+    const int sub = ((x & 7) << 3) | (z & 7);
+    s.seg16[(chi - 1) * 64 + sub] = (uint8_t)(kb >> 8);
+    const int w = z + 32 * x;
+    if (chi > 1) {
+        s.seg16[(chi - 2) * 64 + sub] = (uint8_t)kb;
+        reinterpret_cast<uint16_t *>(s.mask32)[2 * w] = (uint16_t)kb;
+    } else {
+        reinterpret_cast<uint8_t *>(s.mask32)[4 * w + 1] = (uint8_t)(kb >> 8);
+    }
+}
+// Level-8 x line (y,z): positional word z*32+y holds its bits x; the coarse
+// 4^3 corner is always kept (FullWaveletTransform.h:165-168).
+__device__ __forceinline__ void emit8(const Shared &s, int y, int z, unsigned kb)
+{
+    if (y < 4 && z < 4) kb |= 0xFu;
+    const int chi = 1 | ((y >= 4) << 1) | ((z >= 4) << 2);
+    const int sub = ((z & 3) << 2) | (y & 3);
+    s.seg8[(chi - 1) * 16 + sub] = (uint8_t)(kb >> 4);
+    if (chi > 1) s.seg8[(chi - 2) * 16 + sub] = (uint8_t)(kb & 0xF);
+    reinterpret_cast<uint8_t *>(s.mask32)[4 * (y + 32 * z)] = (uint8_t)kb;
+}
+
+__device__ __forceinline__ int seg_count(const Shared &s, int i)
+{
+    if (i < kSegBase8) return 64;
+    if (i < kSegBase16) return __popc(s.seg8[i - kSegBase8]);
+    if (i < kSegBase32) return __popc(s.seg16[i - kSegBase16]);
+    return __popc(s.seg32[i - kSegBase32]);
+}
+
+// Exclusive scan of the run counts into s.off; returns the survivor total.
+__device__ __forceinline__ int scan_segments(const Shared &s)
+{
+    constexpr int PER = (kSegs + kNT - 1) / kNT;  // 5
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) swarp[warp] = cnt;
+    const int i0 = threadIdx.x * PER;
+    int c[PER], sum = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        c[k] = (i0 + k < kSegs) ? seg_count(s, i0 + k) : 0;
+        sum += c[k];
+    }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) s.warp[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        int v = lane < kNW ? swarp[lane] : 0;
-        int incl = v;
+        const int v = lane < kNW ? s.warp[lane] : 0;
+        int w = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
+            const int t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
         }
-        if (lane < kNW) swarp[32 + lane] = incl - v;
-        if (lane == kNW - 1) swarp[32 + kNW] = incl;
+        if (lane < kNW) s.warp[32 + lane] = w - v;
+        if (lane == kNW - 1) s.warp[32 + kNW] = w;
     }
     __syncthreads();
-    *total = swarp[32 + kNW];
-    return swarp[32 + warp];
+    int run = s.warp[32 + warp] + incl - sum;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        if (i0 + k < kSegs) s.off[i0 + k] = run;
+        run += c[k];
+    }
+    const int total = s.warp[32 + kNW];
+    __syncthreads();
+    return total;
+}
+
+// Survivor-order slot -> (physical position, run mask, bit within the run,
+// run offset). The 32 slots of a chunk share their level.
+struct Slot {
+    int pos;
+    unsigned mask;
+    int e;
+    int off;
+};
+__device__ __forceinline__ Slot slot_of(const Shared &s, int sidx)
+{
+    Slot r;
+    if (sidx < 64) {  // coarse, z,y,x order (FullWaveletTransform.h:170-173)
+        r.pos = pidx(sidx & 3, (sidx >> 2) & 3, sidx >> 4);
+        r.mask = 0xffffffffu;
+        r.e = 0;
+        r.off = sidx;
+        return r;
+    }
+    if (sidx < 512) {  // level 8: runs of 4 along x
+        const int q = sidx - 64, seg = q >> 2, e = q & 3, c = (seg >> 4) + 1;
+        r.pos = pidx(4 * (c & 1) + e, 4 * ((c >> 1) & 1) + (seg & 3), 4 * (c >> 2) + ((seg >> 2) & 3));
+        r.mask = s.seg8[seg];
+        r.e = e;
+        r.off = s.off[kSegBase8 + seg];
+        return r;
+    }
+    if (sidx < 4096) {  // level 16: runs of 8 along y
+        const int q = sidx - 512, seg = q >> 3, e = q & 7, c = (seg >> 6) + 1;
+        r.pos = pidx(8 * (c >> 2) + ((seg >> 3) & 7), 8 * (c & 1) + e, 8 * ((c >> 1) & 1) + (seg & 7));
+        r.mask = s.seg16[seg];
+        r.e = e;
+        r.off = s.off[kSegBase16 + seg];
+        return r;
+    }
+    // level 32: runs of 16 along z
+    const int q = sidx - 4096, seg = q >> 4, e = q & 15, c = (seg >> 8) + 1;
+    r.pos = pidx(16 * ((c >> 1) & 1) + (seg & 15), 16 * (c >> 2) + ((seg >> 4) & 15), 16 * (c & 1) + e);
+    r.mask = s.seg32[seg];
+    r.e = e;
+    r.off = s.off[kSegBase32 + seg];
+    return r;
 }
 
 template <int KIND>
@@ -118,88 +312,103 @@ encode_kernel(const CzField *fields, int nfields, long long total_blocks, int ze
               uint8_t *stage, int *rec_bytes, unsigned long long *queue)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    float *sb = reinterpret_cast<float *>(smem + kSmBlock);
-    uint8_t *smask = smem + kSmMask;
-    unsigned *sballot = reinterpret_cast<unsigned *>(smem + kSmBallot);
-    int *swarp = reinterpret_cast<int *>(smem + kSmWarp);
+    const Shared s = carve(smem);
     __shared__ long long s_ticket;
-
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t zmask = zerobits > 0 ? ~((1u << zerobits) - 1u) : 0xffffffffu;
 
     if (threadIdx.x == 0) s_ticket = (long long)atomicAdd(queue, 1ull);
     __syncthreads();
     long long g = s_ticket;
-    float4 pf[kPrefetch];
-    if (g < total_blocks) prefetch_block(locate(fields, nfields, g), pf);
+    float4 pf[16];
+    if (g < total_blocks) load_rows(locate(fields, nfields, g), pf);
 
     while (g < total_blocks) {
         const BlockRef ref = locate(fields, nfields, g);
         const float eps = ref.f->eps;
-        __syncthreads();  // the previous block's emit is done with smem
-        stage_block(sb, pf);
-        __syncthreads();
-        forward_transform<KIND, kNT>(sb);
-
-        // next ticket; its loads overlap thresholding and emission
+        __syncthreads();  // the previous block's emission is done with smem
         if (threadIdx.x == 0) s_ticket = (long long)atomicAdd(queue, 1ull);
+        // ---- level 32, x lines straight from the prefetched rows
+        {
+            const int y = threadIdx.x & 31, z = threadIdx.x >> 5;
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                float v[32];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    v[4 * k + 0] = pf[8 * r + k].x;
+                    v[4 * k + 1] = pf[8 * r + k].y;
+                    v[4 * k + 2] = pf[8 * r + k].z;
+                    v[4 * k + 3] = pf[8 * r + k].w;
+                }
+                line_fwd<32, KIND>(v);
+                st_line<32, 0>(s.sb, pidx(0, y, z + 16 * r), v);
+            }
+        }
         __syncthreads();
         const long long gn = s_ticket;
-        if (gn < total_blocks) prefetch_block(locate(fields, nfields, gn), pf);
-
-        // ---- pass 1: keep flags in survivor order, mask bytes, counts
-        int cnt = 0;
-        for (int ch = 0; ch < kChunksPerWarp; ++ch) {
-            const int cidx = warp * kChunksPerWarp + ch;
-            const int s = cidx * 32 + lane;
-            int p;
-            const float v = sb[swz_of_stream(s, p)];
-            const bool keep = s < 64 || fabsf(v) > eps;  // FullWaveletTransform.h:84
-            const unsigned b = __ballot_sync(0xffffffffu, keep);
-            if (lane == 0) sballot[cidx] = b;
-            cnt += __popc(b);
-            // mask bit p is LSB-first in byte p>>3 (WaveletCompressor.cpp:103-111);
-            // level-32 runs are 16 positions along px, level-16 runs 8
-            if (s >= 4096) {
-                if ((lane & 15) == 0) reinterpret_cast<uint16_t *>(smask)[p >> 4] = (uint16_t)(b >> lane);
-            } else if (s >= 512) {
-                if ((lane & 7) == 0) smask[p >> 3] = (uint8_t)(b >> lane);
-            }
+        sweep<32, 1, true, KIND>(s.sb);
+        __syncthreads();
+        // ---- level 32, z lines + run masks
+        for (int l = threadIdx.x; l < 1024; l += kNT) {
+            const int x = l & 31, y = l >> 5;
+            const int base = pidx(x, y, 0);
+            float v[32];
+            ld_line<32, 2>(s.sb, base, v);
+            line_fwd<32, KIND>(v);
+            st_line<32, 2>(s.sb, base, v);
+            emit32(s, x, y, keep_bits<32>(v, eps));
         }
-        // coarse and level-8 positions: the 64 mask bytes with px,py,pz < 8
+        __syncthreads();
+        // the next block's rows load while this one finishes
+        if (gn < total_blocks) load_rows(locate(fields, nfields, gn), pf);
+        // ---- level 16 (z, x, y) on the [0,16)^3 corner
+        sweep<16, 2, true, KIND>(s.sb);
+        __syncthreads();
+        sweep<16, 0, true, KIND>(s.sb);
+        __syncthreads();
+        if (threadIdx.x < 256) {
+            const int x = threadIdx.x & 15, z = threadIdx.x >> 4;
+            const int base = pidx(x, 0, z);
+            float v[16];
+            ld_line<16, 1>(s.sb, base, v);
+            line_fwd<16, KIND>(v);
+            st_line<16, 1>(s.sb, base, v);
+            emit16(s, x, z, keep_bits<16>(v, eps));
+        }
+        __syncthreads();
+        // ---- level 8 (y, z, x) on the [0,8)^3 corner
+        sweep<8, 1, true, KIND>(s.sb);
+        __syncthreads();
+        sweep<8, 2, true, KIND>(s.sb);
+        __syncthreads();
         if (threadIdx.x < 64) {
-            const int py = threadIdx.x & 7, pz = threadIdx.x >> 3;
-            unsigned byte = 0;
-#pragma unroll
-            for (int px = 0; px < 8; ++px) {
-                const bool coarse = px < 4 && py < 4 && pz < 4;
-                byte |= (unsigned)(coarse || fabsf(sb[swz(px, py, pz)]) > eps) << px;
-            }
-            smask[(py + 32 * pz) * 4] = (uint8_t)byte;
+            const int y = threadIdx.x & 7, z = threadIdx.x >> 3;
+            const int base = pidx(0, y, z);
+            float v[8];
+            ld_line<8, 0>(s.sb, base, v);
+            line_fwd<8, KIND>(v);
+            st_line<8, 0>(s.sb, base, v);
+            emit8(s, y, z, keep_bits<8>(v, eps));
         }
-        int S;
-        int base = warp_offsets(swarp, cnt, &S);
+        __syncthreads();
+        // ---- offsets of every run, record header and mask
+        const int S = scan_segments(s);
         const int nb = kMaskBytes + 4 * S;
         uint8_t *slot = stage + (size_t)g * kSlotBytes;
         if (threadIdx.x == 0) {
             *reinterpret_cast<int *>(slot) = nb;
             rec_bytes[g] = nb;
         }
-        {
-            const uint32_t *src = reinterpret_cast<const uint32_t *>(smask);
-            uint32_t *dst = reinterpret_cast<uint32_t *>(slot + 4);
-            for (int i = threadIdx.x; i < kMaskBytes / 4; i += kNT) dst[i] = src[i];
-        }
-        // ---- pass 2: survivors in order, zero-bits, optional byte planes
+        for (int i = threadIdx.x; i < kMaskBytes / 4; i += kNT)
+            reinterpret_cast<uint32_t *>(slot + 4)[i] = s.mask32[i];
+        // ---- survivors in the reference order, zero-bits, byte planes
         uint8_t *pay = slot + 4 + kMaskBytes;
-        for (int ch = 0; ch < kChunksPerWarp; ++ch) {
-            const int cidx = warp * kChunksPerWarp + ch;
-            const unsigned b = sballot[cidx];
-            if ((b >> lane) & 1u) {
-                const int s = cidx * 32 + lane;
-                int p;
-                const uint32_t u = __float_as_uint(sb[swz_of_stream(s, p)]) & zmask;
-                const int k = base + __popc(b & lanemask_lt());
+        for (int ch = warp; ch < 1024; ch += kNW) {
+            const Slot t = slot_of(s, ch * 32 + lane);
+            if ((t.mask >> t.e) & 1u) {
+                const int k = t.off + __popc(t.mask & ((1u << t.e) - 1u));
+                const uint32_t u = __float_as_uint(s.sb[t.pos]) & zmask;
                 if (shuffle) {
                     pay[k] = (uint8_t)u;
                     pay[S + k] = (uint8_t)(u >> 8);
@@ -209,10 +418,50 @@ encode_kernel(const CzField *fields, int nfields, long long total_blocks, int ze
                     reinterpret_cast<uint32_t *>(pay)[k] = u;
                 }
             }
-            base += __popc(b);
         }
         g = gn;
     }
+}
+
+// ------------------------------------------------------------------ decode
+// Run masks from the positional mask words (the inverse of emit32/16/8).
+__device__ __forceinline__ void runs_from_mask(const Shared &s)
+{
+    for (int i = threadIdx.x; i < kSeg32; i += kNT) {
+        const int c = (i >> 8) + 1, sub = i & 255;
+        const int x = 16 * ((c >> 1) & 1) + (sub & 15), y = 16 * (c >> 2) + (sub >> 4);
+        s.seg32[i] = (uint16_t)(s.mask32[x + 32 * y] >> (16 * (c & 1)));
+    }
+    for (int i = threadIdx.x; i < kSeg16; i += kNT) {
+        const int c = (i >> 6) + 1, sub = i & 63;
+        const int x = 8 * (c >> 2) + (sub >> 3), z = 8 * ((c >> 1) & 1) + (sub & 7);
+        s.seg16[i] = (uint8_t)(s.mask32[z + 32 * x] >> (8 * (c & 1)));
+    }
+    for (int i = threadIdx.x; i < kSeg8; i += kNT) {
+        const int c = (i >> 4) + 1, sub = i & 15;
+        const int y = 4 * ((c >> 1) & 1) + (sub & 3), z = 4 * (c >> 2) + (sub >> 2);
+        s.seg8[i] = (uint8_t)((s.mask32[y + 32 * z] >> (4 * (c & 1))) & 0xF);
+    }
+}
+
+struct Payload {
+    const uint8_t *p;
+    int c;  // byte-plane stride (reshuffle3's n/4, WaveletCompressor.cpp:80)
+    bool shuffle;
+    __device__ __forceinline__ float get(int k) const
+    {
+        if (shuffle)
+            return __uint_as_float((uint32_t)p[k] | ((uint32_t)p[c + k] << 8) | ((uint32_t)p[2 * c + k] << 16) |
+                                   ((uint32_t)p[3 * c + k] << 24));
+        return __uint_as_float(reinterpret_cast<const uint32_t *>(p)[k]);
+    }
+};
+
+// Value at bit e of run `seg` (global run index): its survivor or zero.
+__device__ __forceinline__ float run_value(const Shared &s, const Payload &pl, unsigned mask, int seg, int e)
+{
+    if (!((mask >> e) & 1u)) return 0.f;
+    return pl.get(s.off[seg] + __popc(mask & ((1u << e) - 1u)));
 }
 
 template <int KIND>
@@ -221,14 +470,10 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
               const long long *rec_off, int *status, unsigned long long *queue)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    float *sb = reinterpret_cast<float *>(smem + kSmBlock);
-    uint8_t *smask = smem + kSmMask;
-    unsigned *sballot = reinterpret_cast<unsigned *>(smem + kSmBallot);
-    int *swarp = reinterpret_cast<int *>(smem + kSmWarp);
+    const Shared s = carve(smem);
     __shared__ long long s_ticket;
     __shared__ int s_bad;
 
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -243,89 +488,119 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
         const uint8_t *slot = base + (ro < 0 ? 0 : ro);
         const int nb = ro < 0 ? -1 : *reinterpret_cast<const int *>(slot);
         const bool size_ok = nb >= kMaskBytes && nb <= kMaxRecord + 4;
-
-        // deserialize_bitset (WaveletCompressor.cpp:124-150) + popcount
-        int ones = 0;
-        {
-            const uint32_t *src = reinterpret_cast<const uint32_t *>(slot + 4);
-            uint32_t *dst = reinterpret_cast<uint32_t *>(smask);
-            for (int i = threadIdx.x; i < kMaskBytes / 4; i += kNT) {
-                const uint32_t w = size_ok ? src[i] : 0u;
-                dst[i] = w;
-                ones += __popc(w);
-            }
+        // deserialize_bitset (WaveletCompressor.cpp:124-150)
+        for (int i = threadIdx.x; i < kMaskBytes / 4; i += kNT)
+            s.mask32[i] = size_ok ? reinterpret_cast<const uint32_t *>(slot + 4)[i] : 0u;
+        __syncthreads();
+        runs_from_mask(s);
+        // the base case consumes exactly the 64 coarse survivors (:178-189)
+        if (threadIdx.x < 16) {
+            const int y = threadIdx.x & 3, z = threadIdx.x >> 2;
+            if ((s.mask32[y + 32 * z] & 0xFu) != 0xFu) s_bad = 1;
         }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) ones += __shfl_xor_sync(0xffffffffu, ones, o);
-        int expected;
-        warp_offsets(swarp, ones, &expected);
+        __syncthreads();
+        const int expected = scan_segments(s);
         const int payload = nb - kMaskBytes;
         int nel = payload / 4;
         if (nel - expected == 1) nel--;  // :247-250
-        // every coarse bit set (the base case reads 64 survivors, :178-189)
-        if (threadIdx.x < 64) {
-            const int x = threadIdx.x & 3, y = (threadIdx.x >> 2) & 3, z = threadIdx.x >> 4;
-            const int p = x + 32 * (y + 32 * z);
-            if (!((smask[p >> 3] >> (p & 7)) & 1)) s_bad = 1;
-        }
-        __syncthreads();
         const bool ok = size_ok && nel == expected && !s_bad;
         if (threadIdx.x == 0) status[g] = ok ? 0 : -1;
-
-        // pass 1: survivor ranks in the coarse-first order
-        int cnt = 0;
-        for (int ch = 0; ch < kChunksPerWarp; ++ch) {
-            const int cidx = warp * kChunksPerWarp + ch;
-            const int s = cidx * 32 + lane;
-            int px, py, pz;
-            pos_of_stream(s, px, py, pz);
-            const int p = px + 32 * (py + 32 * pz);
-            const bool eat = ok && ((smask[p >> 3] >> (p & 7)) & 1);
-            const unsigned b = __ballot_sync(0xffffffffu, eat);
-            if (lane == 0) sballot[cidx] = b;
-            cnt += __popc(b);
-        }
-        int total;
-        int base = warp_offsets(swarp, cnt, &total);
-        // pass 2: FullTransformEngine::load -- survivors to their positions,
-        // zeros elsewhere; reshuffle3 (:75-93) reads byte planes of c = n/4
-        const uint8_t *pay = slot + 4 + kMaskBytes;
-        const int c = payload / 4;
-        for (int ch = 0; ch < kChunksPerWarp; ++ch) {
-            const int cidx = warp * kChunksPerWarp + ch;
-            const unsigned b = sballot[cidx];
-            const int s = cidx * 32 + lane;
-            int p;
-            const int a = swz_of_stream(s, p);
-            float v = 0.f;
-            if ((b >> lane) & 1u) {
-                const int k = base + __popc(b & lanemask_lt());
-                uint32_t u;
-                if (shuffle)
-                    u = (uint32_t)pay[k] | ((uint32_t)pay[c + k] << 8) | ((uint32_t)pay[2 * c + k] << 16) |
-                        ((uint32_t)pay[3 * c + k] << 24);
-                else
-                    u = reinterpret_cast<const uint32_t *>(pay)[k];
-                v = __uint_as_float(u);
+        Payload pl;
+        pl.p = slot + 4 + kMaskBytes;
+        pl.c = payload / 4;
+        pl.shuffle = shuffle != 0;
+        // ---- level 8 inverse (x, z, y): x lines gather coarse + level-8 runs
+        if (threadIdx.x < 64) {
+            const int y = threadIdx.x & 7, z = threadIdx.x >> 3;
+            float v[8];
+            const int chi = 1 | ((y >= 4) << 1) | ((z >= 4) << 2);
+            const int sub = ((z & 3) << 2) | (y & 3);
+            const int seghi = kSegBase8 + (chi - 1) * 16 + sub;
+            const unsigned mhi = ok ? s.seg8[seghi - kSegBase8] : 0u;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) v[4 + e] = run_value(s, pl, mhi, seghi, e);
+            if (chi > 1) {
+                const int seglo = kSegBase8 + (chi - 2) * 16 + sub;
+                const unsigned mlo = ok ? s.seg8[seglo - kSegBase8] : 0u;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) v[e] = run_value(s, pl, mlo, seglo, e);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) v[e] = ok ? pl.get(e + 4 * y + 16 * z) : 0.f;
             }
-            sb[a] = v;
-            base += __popc(b);
+            line_inv<8, KIND>(v);
+            st_line<8, 0>(s.sb, pidx(0, y, z), v);
         }
         __syncthreads();
-        inverse_transform<KIND, kNT>(sb);
-        // copy_to (WaveletCompressor.h:73-82) into the field, x fastest
+        sweep<8, 2, false, KIND>(s.sb);
+        __syncthreads();
+        sweep<8, 1, false, KIND>(s.sb);
+        __syncthreads();
+        // ---- level 16 inverse (y, x, z): y lines gather level-16 runs
+        if (threadIdx.x < 256) {
+            const int x = threadIdx.x & 15, z = threadIdx.x >> 4;
+            const int b = pidx(x, 0, z);
+            float v[16];
+            const int chi = 1 | ((z >= 8) << 1) | ((x >= 8) << 2);
+            const int sub = ((x & 7) << 3) | (z & 7);
+            const int seghi = kSegBase16 + (chi - 1) * 64 + sub;
+            const unsigned mhi = ok ? s.seg16[seghi - kSegBase16] : 0u;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[8 + e] = run_value(s, pl, mhi, seghi, e);
+            if (chi > 1) {
+                const int seglo = kSegBase16 + (chi - 2) * 64 + sub;
+                const unsigned mlo = ok ? s.seg16[seglo - kSegBase16] : 0u;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) v[e] = run_value(s, pl, mlo, seglo, e);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) v[e] = s.sb[b + e * SY];
+            }
+            line_inv<16, KIND>(v);
+            st_line<16, 1>(s.sb, b, v);
+        }
+        __syncthreads();
+        sweep<16, 0, false, KIND>(s.sb);
+        __syncthreads();
+        sweep<16, 2, false, KIND>(s.sb);
+        __syncthreads();
+        // ---- level 32 inverse (z, y, x): z lines gather level-32 runs
+        for (int l = threadIdx.x; l < 1024; l += kNT) {
+            const int x = l & 31, y = l >> 5;
+            const int b = pidx(x, y, 0);
+            float v[32];
+            const int chi = 1 | ((x >= 16) << 1) | ((y >= 16) << 2);
+            const int sub = ((y & 15) << 4) | (x & 15);
+            const int seghi = kSegBase32 + (chi - 1) * 256 + sub;
+            const unsigned mhi = ok ? s.seg32[seghi - kSegBase32] : 0u;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) v[16 + e] = run_value(s, pl, mhi, seghi, e);
+            if (chi > 1) {
+                const int seglo = kSegBase32 + (chi - 2) * 256 + sub;
+                const unsigned mlo = ok ? s.seg32[seglo - kSegBase32] : 0u;
+#pragma unroll
+                for (int e = 0; e < 16; ++e) v[e] = run_value(s, pl, mlo, seglo, e);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) v[e] = s.sb[b + e * SZ];
+            }
+            line_inv<32, KIND>(v);
+            st_line<32, 2>(s.sb, b, v);
+        }
+        __syncthreads();
+        sweep<32, 1, false, KIND>(s.sb);
+        __syncthreads();
+        // x lines: inverse, then straight to the field (copy_to, WaveletCompressor.h:73-82)
         float *out = const_cast<float *>(ref.f->data);
-        const CzField &f = *ref.f;
-        for (int i = threadIdx.x; i < kBS3 / 4; i += kNT) {
-            const int row = i >> 3, x0 = (i & 7) * 4;
-            const int y = row & 31, z = row >> 5;
-            float4 w;
-            w.x = sb[swz(x0 + 0, y, z)];
-            w.y = sb[swz(x0 + 1, y, z)];
-            w.z = sb[swz(x0 + 2, y, z)];
-            w.w = sb[swz(x0 + 3, y, z)];
-            float *dst = out + ((size_t)(ref.bz * 32 + z) * f.ny + (size_t)(ref.by * 32 + y)) * f.nx + ref.bx * 32 + x0;
-            __stcs(reinterpret_cast<float4 *>(dst), w);
+        for (int l = threadIdx.x; l < 1024; l += kNT) {
+            const int y = l & 31, z = l >> 5;
+            float v[32];
+            ld_line<32, 0>(s.sb, pidx(0, y, z), v);
+            line_inv<32, KIND>(v);
+            float4 *dst = reinterpret_cast<float4 *>(out + row_offset(ref, y, z));
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                __stcs(dst + k, make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
         }
     }
 }

@@ -35,6 +35,11 @@ def test_gpu_lz4_roundtrip(cz, small_field):
     raw, off = O.field_compress(small_field, 1e-3, 1, 4, 1, 0, 1)
     samples = [b"", b"x", bytes(12), bytes(13), bytes(70000), rng.integers(0, 256, 100000, np.uint8).tobytes(),
                (b"0123456789abcdef" * 5000), bytes(raw[off[0]:off[1]]), bytes(raw[off[7]:off[9]])]
+    # short repeats over a small alphabet at every distance (window and
+    # super-window boundaries), and long runs crossing them
+    toks = [rng.integers(0, 8, 7, np.uint8).tobytes() for _ in range(40)]
+    samples.append(b"".join(toks[i] for i in rng.integers(0, 40, 30000)))
+    samples.append(bytes(3000) + rng.integers(0, 256, 2500, np.uint8).tobytes() + bytes(9000) + b"\x01" * 70000)
     L = O.ref(4, 1, "lz4")
     for d in samples:
         z = cz.lz4_compress(d)
