@@ -30,7 +30,9 @@ EXPORTS = [
     "cz_lz4_bound", "cz_lz4_compress", "cz_lz4_decompress",
     "cz_field_compress", "cz_stream_copy", "cz_field_decompress", "cz_batch_compress",
     "cz_file_bytes", "cz_file_image", "cz_compress_to_image", "cz_image_info", "cz_decompress_image",
+    "cz_blocks_compress_noalloc",
 ]
+NOALLOC_MAX_BLOCKS = 16
 
 
 class CzError(RuntimeError):
@@ -86,5 +88,6 @@ def load():
                                        llp]
     L.cz_image_info.argtypes = [vp, C.c_longlong, ip, ip]
     L.cz_decompress_image.argtypes = [vp, vp, C.c_longlong, C.c_int, C.c_int, vp, vp, C.c_longlong]
+    L.cz_blocks_compress_noalloc.argtypes = [vp, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, vp, vp, vp]
     _L = L
     return L

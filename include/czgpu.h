@@ -139,6 +139,23 @@ int cz_field_decompress(cz_ctx *ctx, const uint8_t *d_data, const long long *d_c
 int cz_batch_compress(cz_ctx *ctx, int nfields, const float *const *d_fields, const int *dims /* 3*nfields: nx,ny,nz */,
                       const float *eps, const cz_params *p, void *stream, cz_stream *out);
 
+/* ---- allocation-free block compression (device buffers) --------------- */
+/* No counterpart in the reference. For callers that cannot call cudaMalloc
+ * (applications that hand all device memory to their own pool, pipelines
+ * where an allocation would synchronise the device): compresses nblocks
+ * (1..CZ_NOALLOC_MAX_BLOCKS) 32^3 blocks stacked in d_blocks (block g at
+ * d_blocks + g*32768, x fastest) with the same encode kernel, using a
+ * static device scratch array of the library (~2.2 MB per device, held
+ * until exit) instead of allocating. Record g goes to d_records +
+ * g*CZ_MAX_RECORD, its size to d_nbytes[g]; asynchronous on `stream`, on
+ * the current device. The first call on a device looks up the scratch
+ * address and should come before any stream capture. Calls share the
+ * scratch, so calls that overlap on the GPU race. Returns CZ_E_ARG for
+ * nblocks beyond the maximum. */
+#define CZ_NOALLOC_MAX_BLOCKS 16
+int cz_blocks_compress_noalloc(const float *d_blocks, int nblocks, float eps, int wtype, int zerobits, int shuffle,
+                               uint8_t *d_records, int *d_nbytes, void *stream);
+
 /* ---- .cz files (host memory) ------------------------------------------ */
 /* Size of the .cz image for a compressed stream (header, metadata, LUT). */
 long long cz_file_bytes(cz_ctx *ctx, const cz_stream *s, int nx, int ny, int nz, const cz_params *p);
