@@ -36,7 +36,6 @@ namespace cz {
 
 constexpr int kLzWarps = 4;
 constexpr int kHashLog = 10;
-constexpr int kBatch = 256;  // sequences per decode batch
 constexpr uint32_t kEmpty = 0xffffffffu;
 constexpr int kMinMatch = 4, kLastLiterals = 5, kMfLimit = 12;
 
@@ -114,12 +113,11 @@ __device__ __forceinline__ void next_skip(Skip &k, const uint8_t *src, int L)
 // ------------------------------------------------------------------ encode
 // Per warp, per super-window of kSW positions:
 //   probe  -- 128 positions per step (4 per lane): hash, table lookup and
-//             insert, verification against the stored 4-byte sequence,
-//             match length up to 12 bytes from memory; the result per
-//             position goes to info[]: 0, or offset | (length-4) << 16 |
-//             bit 31 when the match is longer than measured;
-//   walk   -- lane k walks positions [base+64k, base+64k+64) greedily
-//             (take the match at the cursor, jump past it, else step 1);
+//             insert, verification against the stored 4-byte sequence;
+//             the candidate offset per position goes to info[] (0: none);
+//   walk   -- lane k walks positions [base+32k, base+32k+32) greedily
+//             (take the match at the cursor, measure it, jump past it,
+//             else step 1);
 //   merge  -- lane k keeps its sequences that start at or after the end of
 //             the last kept match of lanes < k: the kept matches never
 //             overlap, so the parse stays valid LZ4 without any lane
@@ -127,7 +125,7 @@ __device__ __forceinline__ void next_skip(Skip &k, const uint8_t *src, int L)
 //   emit   -- every lane sizes its kept sequences, a warp scan places them,
 //             every lane writes its own; literal runs longer than 32 bytes
 //             are queued and copied by the whole warp.
-constexpr int kSW = 2048, kSub = kSW / 32, kMaxSeqLane = kSub / 4;
+constexpr int kSW = 1024, kSub = kSW / 32, kMaxSeqLane = kSub / 4;
 
 // exact match length from (p, cand), starting `known` bytes in (lane-local)
 __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, int known, int matchlimit)
@@ -150,7 +148,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
 {
     __shared__ uint2 table_all[kLzWarps][1 << kHashLog];
     __shared__ uint32_t info_all[kLzWarps][kSW];
-    __shared__ uint2 seq_all[kLzWarps][32][kMaxSeqLane];  // (start, off | (len-4) << 16), len < 2^15 else see lens
+    __shared__ uint2 seq_all[kLzWarps][32][kMaxSeqLane];  // (start, offset)
     __shared__ int lens_all[kLzWarps][32][kMaxSeqLane];
     __shared__ int4 longq_all[kLzWarps][64];  // (dst offset, src offset, n, -)
     __shared__ int nlong_all[kLzWarps];
@@ -218,22 +216,8 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     const int p = wpos + j;
                     const int cand = (int)e[j].x;
                     uint32_t v = 0;
-                    if (valid[j] && e[j].x != kEmpty && e[j].y == seq[j] && cand < p && p - cand <= 65535) {
-                        // up to 8 more bytes from memory; longer matches are finished in the walk
-                        const int lim = matchlimit - p;
-                        int len = kMinMatch;
-                        const uint32_t x1 = rd32u(src + p + 4) ^ rd32u(src + cand + 4);
-                        if (x1) {
-                            len += (__ffs(x1) - 1) >> 3;
-                        } else {
-                            len += 4;
-                            const uint32_t x2 = rd32u(src + p + 8) ^ rd32u(src + cand + 8);
-                            len += x2 ? ((__ffs(x2) - 1) >> 3) : 4;
-                        }
-                        const bool more = len == 12 && len < lim;
-                        if (len > lim) len = lim;
-                        v = (uint32_t)(p - cand) | ((uint32_t)(len - kMinMatch) << 16) | (more ? 0x80000000u : 0u);
-                    }
+                    if (valid[j] && e[j].x != kEmpty && e[j].y == seq[j] && cand < p && p - cand <= 65535)
+                        v = (uint32_t)(p - cand);  // the walk measures the length of chosen matches
                     if (valid[j]) info[p - base] = v;
                     any_match |= v != 0;
                 }
@@ -254,9 +238,8 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 while (q < qe) {
                     const uint32_t v = info[q - base];
                     if (v) {
-                        int len = kMinMatch + (int)((v >> 16) & 0x7fff);
-                        const int off = (int)(v & 0xffff);
-                        if (v & 0x80000000u) len = match_len(src, q, q - off, len, matchlimit);
+                        const int off = (int)v;
+                        const int len = match_len(src, q, q - off, kMinMatch, matchlimit);
                         myseq[ns] = make_uint2((uint32_t)q, (uint32_t)off);
                         mylen[ns] = len;
                         ++ns;
@@ -376,146 +359,351 @@ __device__ __forceinline__ long long get_len(const uint8_t *src, int &ip, int li
     return sum;
 }
 
-// Where the byte at output position s of a batch comes from: a literal of
-// the batch, or a byte before the batch. Matches are followed back through
-// their (periodic) sources; each step lands before the match it left.
-__device__ __forceinline__ int resolve(const int4 *batch, int n, int batch_end, int s)
+// Parallel parse. The decoder reads a window of kWin input bytes starting
+// at the current sequence. Every lane decodes the token at 4 candidate
+// positions as if a sequence started there (literal length, offset, match
+// length, position of the next token); only the candidates reachable from
+// the window's first position are real sequences. Jump tables T_b (2^b
+// steps along the next-token chain, built by pointer doubling in shared
+// memory) let lane k find the k-th sequence directly. Candidates whose
+// length fields run longer than kFastExt continuation bytes are flagged
+// and decoded serially when the chain reaches them.
+constexpr int kWin = 128, kFastExt = 8, kExit = kWin;
+// Output ring per warp: the last kRing bytes of output. A window adds at
+// most kStage bytes, so at least kRing - kStage bytes of history stay
+// readable while it is written (about 99% of match sources in block-record
+// chunks lie within 3 KB).
+constexpr int kRing = 4096, kMask = kRing - 1, kStage = 1024;
+constexpr int kTermIn = 1 << 16, kSlow = 1 << 17;  // flags above the 16-bit offset
+
+// Continuation bytes like get_len, at most kFastExt of them: false if the
+// field is longer (the caller then decodes the sequence serially).
+__device__ __forceinline__ bool get_len_fast(const uint8_t *src, int &ip, int lim, int &sum)
 {
-    const int b0 = batch[0].z;
-    while (s >= b0) {
-        int lo = 0, hi = n - 1;  // last sequence whose output starts at or before s
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (batch[mid].z <= s) lo = mid;
-            else hi = mid - 1;
-        }
-        const int4 q = batch[lo];
-        const int ms = q.z + q.y;
-        if (s < ms) break;  // a literal of this batch
-        s = ms - q.w + (s - ms) % q.w;
+#pragma unroll 1
+    for (int k = 0; k < kFastExt; ++k) {
+        if (ip >= lim) return true;
+        const int s = __ldg(src + ip++);
+        sum += s;
+        if (s != 255) return true;
     }
-    (void)batch_end;
-    return s;
+    return ip >= lim;
+}
+
+// n <= 8 bytes from read-only input into the ring at output position o;
+// all loads before the stores.
+__device__ __forceinline__ void copy_lit(uint8_t *ring, int o, const uint8_t *s, int n)
+{
+    uint8_t b[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) b[j] = j < n ? __ldg(s + j) : (uint8_t)0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (j < n) ring[(o + j) & kMask] = b[j];
+}
+
+// Byte k of a match at output ms comes from ms - off + (k mod off): the
+// byte-serial copy repeats the first `off` bytes when off < length.
+__device__ __forceinline__ int msrc(int k, int off, int ml) { return off >= ml ? k : k % off; }
+
+// Output byte x, x < the window's start: from the ring when it is still
+// held there (x >= lo), else from the output in global memory (via L2).
+__device__ __forceinline__ uint8_t out_byte(const uint8_t *ring, const uint8_t *dst, int x, int lo)
+{
+    return x >= lo ? ring[x & kMask] : __ldcg(dst + x);
+}
+
+// ml <= 8 bytes of a match at ms whose sources lie before the window and
+// in the ring; r runs through the source positions modulo off.
+__device__ __forceinline__ void copy_match(uint8_t *ring, int ms, int off, int ml)
+{
+    uint8_t b[8];
+    int r = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        b[j] = j < ml ? ring[(ms - off + r) & kMask] : (uint8_t)0;
+        r = r + 1 == off ? 0 : r + 1;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (j < ml) ring[(ms + j) & kMask] = b[j];
+}
+
+// n bytes of the ring starting at ring offset r (r + n <= kRing) to d (any
+// alignment): 4-byte stores once d is aligned.
+__device__ __forceinline__ void flush(uint8_t *d, const uint8_t *ring, int r, int n, int lane)
+{
+    int h = (int)((4 - (reinterpret_cast<uintptr_t>(d) & 3)) & 3);
+    if (h > n) h = n;
+    if (lane < h) d[lane] = ring[r + lane];
+    const int nw = (n - h) >> 2, b = r + h, sh = 8 * (b & 3);
+    const uint32_t *sw = reinterpret_cast<const uint32_t *>(ring) + (b >> 2);
+    uint32_t *dw = reinterpret_cast<uint32_t *>(d + h);
+    for (int i = lane; i < nw; i += 32) dw[i] = sh ? __funnelshift_r(sw[i], sw[i + 1], sh) : sw[i];
+    const int t = (n - h) & 3;
+    if (lane < t) d[h + 4 * nw + lane] = ring[b + 4 * nw + lane];
 }
 
 __global__ void __launch_bounds__(128)
 lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
                   uint8_t *__restrict__ out, const long long *out_off, const int *out_cap, int *out_len)
 {
-    // per warp: a batch of sequences (literal source, literal length,
-    // output position, offset); a match runs to the next output position
-    __shared__ int4 batch_all[4][kBatch + 1];
+    __shared__ int4 cand_all[4][kWin];           // (literal start, literal length, match length, offset | flags)
+    __shared__ int next_all[4][kWin];            // input position after the candidate's sequence
+    __shared__ __align__(16) uint8_t jump_all[4][5][kWin + 4];  // T_b; kExit: leaves the window
+    __shared__ __align__(16) uint8_t ring_all[4][kRing + 16];  // recent output (16 bytes of slack)
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    int4 *batch = batch_all[wib];
+    int4 *cand = cand_all[wib];
+    int *nextp = next_all[wib];
+    uint8_t(*T)[kWin + 4] = jump_all[wib];
+    uint8_t *ring = ring_all[wib];
+    if (lane < 4) {
+#pragma unroll
+        for (int b = 0; b < 5; ++b) T[b][kWin + lane] = (uint8_t)kExit;
+    }
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int c = gw; c < nchunks; c += nw) {
         const uint8_t *src = in + in_off[c];
         const int iend = in_len[c];
         uint8_t *dst = out + out_off[c];
         const int oend = out_cap[c];
-        int ip = 0, op = 0, err = 0, done = 0;
+        int s0 = 0, op = 0, err = 0, ring_lo = 0;  // output before ring_lo is not in the ring
+        bool done = false;
         if (iend <= 0) {
             if (lane == 0) out_len[c] = 0;  // lz4.c:836: error exit at position 0
             continue;
         }
         while (!done && !err) {
-            // ---- token walk (lane 0)
-            int n = 0, last_src = 0, last_len = 0;
-            if (lane == 0) {
-                while (n < kBatch) {
-                    const int token = src[ip++];
-                    long long len = token >> 4;
-                    if (len == 15) len += get_len(src, ip, iend);
-                    // lz4.c:851-858: the last sequence holds only literals and ends the input
-                    if (len > (long long)(oend - op - kMfLimit) || len > (long long)(iend - ip - (2 + 1 + kLastLiterals))) {
-                        if (len > (long long)(oend - op) || len != (long long)(iend - ip)) {
-                            err = 1;
-                        } else {
-                            last_src = ip;
-                            last_len = (int)len;
-                            done = 1;
-                        }
-                        break;
+            // ---- candidates s0 + 4*lane + j; the next window's input into L1
+            if (lane < 2 && s0 + kWin + 128 * lane < iend)
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(src + s0 + kWin + 128 * lane));
+            {  // phase-major over the 4 candidates, so that their loads overlap
+                int tok[4], ip[4], lit[4], ml[4], off[4], nx[4];
+                bool more[4], stat[4];  // stat: a plain sequence so far
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int p = s0 + 4 * lane + j;
+                    tok[j] = p < iend ? (int)__ldg(src + p) : -1;
+                    ip[j] = p + 1;
+                    lit[j] = (tok[j] >> 4) & 15;
+                    ml[j] = tok[j] & 15;
+                    off[j] = 0;
+                    nx[j] = 0;
+                }
+                // literal length continuation (lz4.c:846-850): the first byte
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    more[j] = false;
+                    if (tok[j] >= 0 && lit[j] == 15 && ip[j] < iend) {
+                        const int e = __ldg(src + ip[j]);
+                        ++ip[j];
+                        lit[j] += e;
+                        more[j] = e == 255;
                     }
-                    const int lsrc = ip, lpos = op;
-                    op += (int)len;
-                    ip += (int)len;
-                    const int off = (int)src[ip] | ((int)src[ip + 1] << 8);
+                }
+                // ... and the rare longer ones
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    stat[j] = tok[j] >= 0;
+                    if (more[j]) stat[j] = get_len_fast(src, ip[j], iend, lit[j]);
+                }
+                int flags[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    flags[j] = 0;
+                    if (tok[j] >= 0) {
+                        if (!stat[j]) flags[j] = kSlow;
+                        else if (lit[j] > iend - ip[j] - (2 + 1 + kLastLiterals)) flags[j] = kTermIn;  // lz4.c:851
+                    }
+                    stat[j] = tok[j] >= 0 && flags[j] == 0;
+                    if (stat[j]) {
+                        const int ipo = ip[j] + lit[j];
+                        off[j] = (int)__ldg(src + ipo) | ((int)__ldg(src + ipo + 1) << 8);
+                        nx[j] = ipo + 2;
+                    }
+                }
+                // match length continuation (lz4.c:873-882)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    more[j] = false;
+                    if (stat[j] && ml[j] == 15 && nx[j] < iend - (kLastLiterals + 1)) {
+                        const int e = __ldg(src + nx[j]);
+                        ++nx[j];
+                        ml[j] += e;
+                        more[j] = e == 255;
+                    }
+                }
+                uint32_t tword = 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (more[j] && !get_len_fast(src, nx[j], iend - (kLastLiterals + 1), ml[j])) flags[j] = kSlow;
+                    ml[j] += kMinMatch;
+                    int t = kExit;
+                    if (stat[j] && flags[j] == 0 && nx[j] - s0 < kWin) t = nx[j] - s0;
+                    if (flags[j]) nx[j] = 0;
+                    cand[4 * lane + j] = make_int4(ip[j], lit[j], ml[j], off[j] | flags[j]);
+                    nextp[4 * lane + j] = nx[j];
+                    tword |= (uint32_t)t << (8 * j);
+                }
+                reinterpret_cast<uint32_t *>(T[0])[lane] = tword;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int b = 1; b < 5; ++b) {
+                const uint32_t w = reinterpret_cast<const uint32_t *>(T[b - 1])[lane];
+                uint32_t v = 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) v |= (uint32_t)T[b - 1][(w >> (8 * j)) & 0xff] << (8 * j);
+                __syncwarp();
+                reinterpret_cast<uint32_t *>(T[b])[lane] = v;
+                __syncwarp();
+            }
+            // ---- lane k takes the k-th sequence of the chain
+            int pos = 0;
+#pragma unroll
+            for (int b = 0; b < 5; ++b)
+                if ((lane >> b) & 1) pos = T[b][pos];
+            const bool member = pos < kWin;
+            const int nm = __popc(__ballot_sync(0xffffffffu, member));
+            int4 q = make_int4(0, 0, 0, 0);
+            int nx = 0;
+            if (member) {
+                q = cand[pos];
+                nx = nextp[pos];
+            }
+            const int flags = q.w & ~0xffff, off = q.w & 0xffff;
+            const bool term_in = flags & kTermIn, slow = flags & kSlow;
+            int len = member && !slow ? q.y + (term_in ? 0 : q.z) : 0;
+            int incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int opl = op + incl - len, ms = opl + q.y;
+            // ---- acceptance tests in sequence order (lz4.c:851-858, :868, :888-890)
+            int stop = 0, epos = 0;  // 1: end of input, 2: malformed, 3: decode serially
+            if (member) {
+                if (slow) {
+                    stop = 3;
+                } else if (term_in || q.y > oend - opl - kMfLimit) {
+                    if (q.y > oend - opl || q.y != iend - q.x) {
+                        stop = 2;
+                        epos = q.x;
+                    } else {
+                        stop = 1;
+                    }
+                } else if (off == 0 || off > ms) {
+                    stop = 2;
+                    epos = q.x + q.y + 2;
+                } else if (q.z > oend - ms - kLastLiterals) {
+                    stop = 2;
+                    epos = nx;
+                }
+            }
+            const unsigned sb = __ballot_sync(0xffffffffu, stop != 0);
+            int ks = sb ? __ffs(sb) - 1 : nm;  // first sequence not taken as a plain one
+            int kstop = __shfl_sync(0xffffffffu, stop, ks & 31);
+            const int kepos = __shfl_sync(0xffffffffu, epos, ks & 31);
+            // the window's output is staged in shared memory: sequences that
+            // do not fit go to the serial path
+            const unsigned fb = __ballot_sync(0xffffffffu, member && incl > kStage);
+            if (fb && __ffs(fb) - 1 <= ks) {
+                ks = __ffs(fb) - 1;
+                kstop = 3;
+            }
+            // sequences [0, ks) are complete; sequence ks contributes its
+            // literals when it ends the input
+            const bool lits = lane < ks || (lane == ks && kstop == 1);
+            const bool mat = lane < ks;
+            if (lits && q.y <= 8) copy_lit(ring, opl, src + q.x, q.y);
+            unsigned pend = __ballot_sync(0xffffffffu, lits && q.y > 8);
+            while (pend) {
+                const int who = __ffs(pend) - 1;
+                pend &= pend - 1;
+                const int o0 = __shfl_sync(0xffffffffu, opl, who);
+                const int x0 = __shfl_sync(0xffffffffu, q.x, who);
+                const int n0 = __shfl_sync(0xffffffffu, q.y, who);
+                for (int k = lane; k < n0; k += 32) ring[(o0 + k) & kMask] = __ldg(src + x0 + k);
+            }
+            // matches whose sources lie before the window and are still in
+            // the ring are copied by their lane; the others replay in order
+            // (in-window sources, sources in global memory, long matches)
+            const int lo = max(ring_lo, op + kStage - kRing);  // not overwritten by this window
+            const bool fast = mat && q.z <= 8 && ms - off + min(q.z, off) <= op && ms - off >= lo;
+            if (fast) copy_match(ring, ms, off, q.z);
+            __syncwarp();
+            pend = __ballot_sync(0xffffffffu, mat && !fast);
+            while (pend) {
+                const int who = __ffs(pend) - 1;
+                pend &= pend - 1;
+                const int m0 = __shfl_sync(0xffffffffu, ms, who);
+                const int o0 = __shfl_sync(0xffffffffu, off, who);
+                const int l0 = __shfl_sync(0xffffffffu, q.z, who);
+                for (int k = lane; k < l0; k += 32) {
+                    const int x = m0 - o0 + msrc(k, o0, l0);
+                    ring[(m0 + k) & kMask] = out_byte(ring, dst, x, lo);
+                }
+                __syncwarp();
+            }
+            const int nout = kstop == 1 ? __shfl_sync(0xffffffffu, opl + q.y, ks & 31) - op
+                                        : (ks > 0 ? __shfl_sync(0xffffffffu, incl, ks - 1) : 0);
+            {
+                const int r = op & kMask, n1 = min(nout, kRing - r);
+                flush(dst + op, ring, r, n1, lane);
+                if (nout > n1) flush(dst + op + n1, ring, 0, nout - n1, lane);
+            }
+            __syncwarp();
+            // ---- advance
+            op += nout;
+            if (kstop == 1) {
+                done = true;
+            } else if (kstop == 2) {
+                err = kepos;
+            } else if (kstop == 3) {
+                // a sequence with long length fields, decoded serially
+                int ip = __shfl_sync(0xffffffffu, s0 + pos, ks & 31);
+                const int token = src[ip++];
+                long long ll = token >> 4;
+                if (ll == 15) ll += get_len(src, ip, iend);
+                if (ll > (long long)(oend - op - kMfLimit) || ll > (long long)(iend - ip - (2 + 1 + kLastLiterals))) {
+                    if (ll > (long long)(oend - op) || ll != (long long)(iend - ip)) {
+                        err = ip;
+                    } else {
+                        warp_copy(dst + op, src + ip, (int)ll, lane);
+                        op += (int)ll;
+                        done = true;
+                    }
+                } else {
+                    warp_copy(dst + op, src + ip, (int)ll, lane);
+                    op += (int)ll;
+                    ip += (int)ll;
+                    const int o = (int)src[ip] | ((int)src[ip + 1] << 8);
                     ip += 2;
-                    if (off == 0 || off > op) {
-                        err = 1;
-                        break;
+                    if (o == 0 || o > op) {
+                        err = ip;
+                    } else {
+                        long long m = token & 15;
+                        if (m == 15) m += get_len(src, ip, iend - (kLastLiterals + 1));
+                        m += kMinMatch;
+                        if (m > (long long)(oend - op - kLastLiterals)) {
+                            err = ip;
+                        } else {
+                            __syncwarp();
+                            for (int k = lane; k < (int)m; k += 32) dst[op + k] = __ldcg(dst + op - o + msrc(k, o, (int)m));
+                            __syncwarp();
+                            op += (int)m;
+                            s0 = ip;
+                            ring_lo = op;  // written around the ring
+                        }
                     }
-                    long long ml = token & 15;
-                    if (ml == 15) ml += get_len(src, ip, iend - (kLastLiterals + 1));  // lz4.c:873-882
-                    ml += kMinMatch;
-                    if (ml > (long long)(oend - op - kLastLiterals)) {  // lz4.c:888-890
-                        err = 1;
-                        break;
-                    }
-                    batch[n++] = make_int4(lsrc, (int)len, lpos, off);
-                    op += (int)ml;
                 }
-                batch[n] = make_int4(0, 0, op, 1);  // sentinel: end of the last match
-            }
-            n = __shfl_sync(0xffffffffu, n, 0);
-            ip = __shfl_sync(0xffffffffu, ip, 0);
-            op = __shfl_sync(0xffffffffu, op, 0);
-            err = __shfl_sync(0xffffffffu, err, 0);
-            done = __shfl_sync(0xffffffffu, done, 0);
-            last_src = __shfl_sync(0xffffffffu, last_src, 0);
-            last_len = __shfl_sync(0xffffffffu, last_len, 0);
-            __syncwarp();
-            if (err) break;
-            // ---- literals: one sequence per lane, long runs by the warp
-            for (int b0 = 0; b0 < n; b0 += 32) {
-                const int k = b0 + lane;
-                int4 q = make_int4(0, 0, 0, 1);
-                if (k < n) q = batch[k];
-                if (q.y <= 32) {
-                    for (int i = 0; i < q.y; ++i) dst[q.z + i] = src[q.x + i];
-                }
-                unsigned pend = __ballot_sync(0xffffffffu, q.y > 32);
-                while (pend) {
-                    const int who = __ffs(pend) - 1;
-                    pend &= pend - 1;
-                    const int xs = __shfl_sync(0xffffffffu, q.x, who);
-                    const int yl = __shfl_sync(0xffffffffu, q.y, who);
-                    const int zp = __shfl_sync(0xffffffffu, q.z, who);
-                    warp_copy(dst + zp, src + xs, yl, lane);
-                }
+            } else {
+                s0 = __shfl_sync(0xffffffffu, nx, nm - 1);
             }
             __syncwarp();
-            // ---- matches: every byte resolves its source independently
-            for (int b0 = 0; b0 < n; b0 += 32) {
-                const int k = b0 + lane;
-                int ms = 0, me = 0, off = 1;
-                if (k < n) {
-                    const int4 q = batch[k];
-                    ms = q.z + q.y;
-                    me = batch[k + 1].z;
-                    off = q.w;
-                }
-                if (me - ms <= 32) {
-                    for (int t = ms; t < me; ++t) dst[t] = __ldcg(dst + resolve(batch, n, op, t - off));
-                }
-                unsigned pend = __ballot_sync(0xffffffffu, me - ms > 32);
-                while (pend) {
-                    const int who = __ffs(pend) - 1;
-                    pend &= pend - 1;
-                    const int s0 = __shfl_sync(0xffffffffu, ms, who);
-                    const int e0 = __shfl_sync(0xffffffffu, me, who);
-                    const int o0 = __shfl_sync(0xffffffffu, off, who);
-                    for (int t = s0 + lane; t < e0; t += 32) dst[t] = __ldcg(dst + resolve(batch, n, op, t - o0));
-                }
-            }
-            __syncwarp();
-            if (done) {
-                for (int i = lane; i < last_len; i += 32) dst[op + i] = src[last_src + i];
-                op += last_len;
-            }
         }
-        if (lane == 0) out_len[c] = err ? -(ip > 0 ? ip : 1) : op;
+        if (lane == 0) out_len[c] = err ? -err : op;
         __syncwarp();
     }
 }

@@ -79,3 +79,59 @@ def zlib_chunks(raw, off, bpc, nblocks):
         c1 = min(nblocks, c0 + bpc)
         out.append(zlib.compress(bytes(raw[off[c0]:off[c1]]), 6))
     return out
+
+
+def _lz4_len(out, n):
+    """LZ4 length continuation bytes for n >= 15 (n - 15 as 255s and a rest)."""
+    n -= 15
+    while n >= 255:
+        out.append(255)
+        n -= 255
+    out.append(n)
+
+
+def lz4_random_stream(rng, nseq, final_lit=12):
+    """A valid LZ4 block built sequence by sequence, and its decoded bytes.
+
+    Literal and match lengths mix the common short ones with lengths that
+    need continuation bytes (a few long enough to need more than eight),
+    offsets mix 1..8 (overlapping, byte-periodic copies), distances inside
+    a 128-byte input window and far ones; the last literal run is at least
+    12 bytes, so the stream is accepted with an output capacity equal to
+    its decoded size."""
+    z = bytearray()
+    out = bytearray()
+    for i in range(nseq):
+        r = rng.random()
+        lit = int(rng.integers(0, 4)) if r < 0.7 else int(rng.integers(14, 40)) if r < 0.93 else \
+            int(rng.integers(250, 700)) if r < 0.99 else int(rng.integers(2100, 5000))
+        if not out and lit == 0:
+            lit = 1
+        r = rng.random()
+        ml = int(rng.integers(4, 9)) if r < 0.7 else int(rng.integers(15, 40)) if r < 0.93 else \
+            int(rng.integers(250, 700)) if r < 0.99 else int(rng.integers(2100, 5000))
+        lits = rng.integers(0, 256, lit, np.uint8).tobytes()
+        have = len(out) + lit
+        r = rng.random()
+        off = int(rng.integers(1, 9)) if r < 0.3 else int(rng.integers(9, 200)) if r < 0.7 else \
+            int(rng.integers(200, 65536))
+        off = max(1, min(off, have, 65535))
+        tok = (min(lit, 15) << 4) | min(ml - 4, 15)
+        z.append(tok)
+        if lit >= 15:
+            _lz4_len(z, lit)
+        z += lits
+        z += bytes((off & 255, off >> 8))
+        if ml - 4 >= 15:
+            _lz4_len(z, ml - 4)
+        out += lits
+        for k in range(ml):
+            out.append(out[len(out) - off])
+    lit = final_lit + int(rng.integers(0, 40))
+    lits = rng.integers(0, 256, lit, np.uint8).tobytes()
+    z.append(min(lit, 15) << 4)
+    if lit >= 15:
+        _lz4_len(z, lit)
+    z += lits
+    out += lits
+    return bytes(z), bytes(out)

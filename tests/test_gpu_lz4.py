@@ -71,3 +71,22 @@ def test_gpu_lz4_rejects_malformed(cz):
         except cz.CzError:
             n, _ = O.lz4_decompress(junk, 4096)
             assert n <= 0
+
+
+def test_gpu_lz4_decodes_constructed_streams(cz):
+    """Valid streams with overlapping copies, every offset class and long
+    length fields decode as the restated reference decoder decodes them;
+    with one byte less of output capacity both reject them."""
+    from tests.helpers import lz4_random_stream
+    rng = np.random.default_rng(21)
+    for t in range(40):
+        z, ref = lz4_random_stream(rng, int(rng.integers(1, 400)))
+        n, o = O.lz4_decompress(z, len(ref))
+        assert n == len(ref) and o.tobytes() == ref  # the construction is valid
+        assert cz.lz4_decompress(z, len(ref)) == ref
+        assert cz.lz4_decompress(z, len(ref) + 100) == ref
+        for cap in (len(ref) - 1, len(ref) // 2):
+            n, _ = O.lz4_decompress(z, cap)
+            assert n <= 0
+            with pytest.raises(cz.CzError):
+                cz.lz4_decompress(z, cap)
