@@ -125,7 +125,12 @@ __device__ __forceinline__ void next_skip(Skip &k, const uint8_t *src, int L)
 //   emit   -- every lane sizes its kept sequences, a warp scan places them,
 //             every lane writes its own; literal runs longer than 32 bytes
 //             are queued and copied by the whole warp.
-constexpr int kSW = 1024, kSub = kSW / 32, kMaxSeqLane = kSub / 4;
+constexpr int kSW = 512, kSub = kSW / 32, kMaxSeqLane = kSub / 4;
+// Hash table entry: position modulo 2^18 in the high bits, a 14-bit tag of
+// the 4-byte sequence in the low bits. A tag hit is only a candidate: the
+// walk measures the match from its first byte and drops it below 4 bytes.
+constexpr uint32_t kPosMask = (1u << 18) - 1;
+__device__ __forceinline__ uint32_t lz_tag(uint32_t v) { return (v * 0x85ebca77u) >> 18; }
 
 // exact match length from (p, cand), starting `known` bytes in (lane-local)
 __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, int known, int matchlimit)
@@ -146,16 +151,16 @@ __global__ void __launch_bounds__(kLzWarps * 32)
 lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
                   uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records)
 {
-    __shared__ uint2 table_all[kLzWarps][1 << kHashLog];
-    __shared__ uint32_t info_all[kLzWarps][kSW];
-    __shared__ uint2 seq_all[kLzWarps][32][kMaxSeqLane];  // (start, offset)
+    __shared__ uint32_t table_all[kLzWarps][1 << kHashLog];
+    __shared__ uint16_t info_all[kLzWarps][kSW];                // candidate offset per position, 0: none
+    __shared__ uint32_t seq_all[kLzWarps][32][kMaxSeqLane];     // start - base | offset << 16
     __shared__ int lens_all[kLzWarps][32][kMaxSeqLane];
-    __shared__ int4 longq_all[kLzWarps][64];  // (dst offset, src offset, n, -)
+    __shared__ int4 longq_all[kLzWarps][32];  // (dst offset, src offset, n, -)
     __shared__ int nlong_all[kLzWarps];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    uint2 *table = table_all[wib];
-    uint32_t *info = info_all[wib];
-    uint2 *myseq = seq_all[wib][lane];
+    uint32_t *table = table_all[wib];
+    uint16_t *info = info_all[wib];
+    uint32_t *myseq = seq_all[wib][lane];
     int *mylen = lens_all[wib][lane];
     int4 *longq = longq_all[wib];
     int &nlong = nlong_all[wib];
@@ -166,7 +171,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
         const int L = in_len[c];
         uint8_t *dst = out + out_off[c];
         const int cap = L + L / 255 + 16;
-        for (int i = lane; i < (1 << kHashLog); i += 32) table[i] = make_uint2(kEmpty, 0u);
+        for (int i = lane; i < (1 << kHashLog); i += 32) table[i] = kEmpty;
         __syncwarp();
         int pos = 0, anchor = 0, op = 0, miss = 0;
         bool overflow = false;
@@ -203,22 +208,25 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     seq[j] = j ? __funnelshift_r(w0, w1, 8 * j) : w0;
                     h[j] = lz_hash(seq[j]);
                 }
-                uint2 e[4];
+                uint32_t e[4], tag[4];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) e[j] = table[h[j]];
+                for (int j = 0; j < 4; ++j) {
+                    e[j] = table[h[j]];
+                    tag[j] = lz_tag(seq[j]);
+                }
                 __syncwarp();
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
-                    if (valid[j]) table[h[j]] = make_uint2((uint32_t)(wpos + j), seq[j]);
+                    if (valid[j]) table[h[j]] = (((uint32_t)(wpos + j) & kPosMask) << 14) | tag[j];
                 __syncwarp();
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int p = wpos + j;
-                    const int cand = (int)e[j].x;
-                    uint32_t v = 0;
-                    if (valid[j] && e[j].x != kEmpty && e[j].y == seq[j] && cand < p && p - cand <= 65535)
-                        v = (uint32_t)(p - cand);  // the walk measures the length of chosen matches
-                    if (valid[j]) info[p - base] = v;
+                    const int off = (int)(((uint32_t)p - (e[j] >> 14)) & kPosMask);
+                    int v = 0;
+                    if (valid[j] && e[j] != kEmpty && (e[j] & 0x3fff) == tag[j] && off >= 1 && off <= 65535 && off <= p)
+                        v = off;  // the walk verifies and measures chosen candidates
+                    if (valid[j]) info[p - base] = (uint16_t)v;
                     any_match |= v != 0;
                 }
             }
@@ -236,11 +244,10 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 int q = w0p;
                 const int qe = min(w0p + kSub, end);
                 while (q < qe) {
-                    const uint32_t v = info[q - base];
-                    if (v) {
-                        const int off = (int)v;
-                        const int len = match_len(src, q, q - off, kMinMatch, matchlimit);
-                        myseq[ns] = make_uint2((uint32_t)q, (uint32_t)off);
+                    const int off = info[q - base];
+                    const int len = off ? match_len(src, q, q - off, 0, matchlimit) : 0;
+                    if (len >= kMinMatch) {
+                        myseq[ns] = (uint32_t)(q - base) | (uint32_t)off << 16;
                         mylen[ns] = len;
                         ++ns;
                         if (first_start > q) first_start = q;
@@ -252,18 +259,28 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     }
                 }
             }
-            // ---- merge: P_k = end of the last kept match of lanes < k
-            int P = anchor, myP = anchor;
-            for (int k = 0; k < 32; ++k) {
-                const int ls = __shfl_sync(0xffffffffu, last_start, k);
-                const int le = __shfl_sync(0xffffffffu, last_end, k);
-                if (lane == k) myP = P;
-                if (ls >= P) P = le;
+            // ---- merge: P_k = end of the last kept match of lanes < k.
+            // Usually every lane keeps its last sequence, so P_k is the end
+            // of the nearest lower lane's last match; where a match reaches
+            // past a later lane's last start, the exact serial rule runs.
+            const unsigned has = __ballot_sync(0xffffffffu, ns > 0);
+            const unsigned lower = has & lanemask_lt_();
+            int myP = __shfl_sync(0xffffffffu, last_end, lower ? 31 - __clz(lower) : 0);
+            if (!lower) myP = anchor;
+            int P = has ? __shfl_sync(0xffffffffu, last_end, 31 - __clz(has)) : anchor;
+            if (__any_sync(0xffffffffu, ns > 0 && last_start < myP)) {
+                P = anchor;
+                for (int k = 0; k < 32; ++k) {
+                    const int ls = __shfl_sync(0xffffffffu, last_start, k);
+                    const int le = __shfl_sync(0xffffffffu, last_end, k);
+                    if (lane == k) myP = P;
+                    if (ls >= P) P = le;
+                }
             }
             // ---- emit: kept sequences are those starting at or after myP
             int lit_from = myP, bytes = 0, nkeep = 0;
             for (int i = 0; i < ns; ++i) {
-                const int st = (int)myseq[i].x;
+                const int st = base + (int)(myseq[i] & 0xffff);
                 if (st < lit_from) continue;
                 const int l = st - lit_from, ml = mylen[i] - kMinMatch;
                 bytes += 1 + (l >= 15 ? len_bytes(l - 15) : 0) + l + 2 + (ml >= 15 ? len_bytes(ml - 15) : 0);
@@ -287,9 +304,9 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 int at = op + incl - bytes;
                 lit_from = myP;
                 for (int i = 0; i < ns; ++i) {
-                    const int st = (int)myseq[i].x;
+                    const int st = base + (int)(myseq[i] & 0xffff);
                     if (st < lit_from) continue;
-                    const int l = st - lit_from, ml = mylen[i] - kMinMatch, off = (int)myseq[i].y;
+                    const int l = st - lit_from, ml = mylen[i] - kMinMatch, off = (int)(myseq[i] >> 16);
                     uint8_t *d = dst + at;
                     *d++ = (uint8_t)(((l >= 15 ? 15 : l) << 4) | (ml >= 15 ? 15 : ml));
                     if (l >= 15) {
@@ -300,7 +317,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                         for (int b = 0; b < l; ++b) d[b] = src[lit_from + b];
                     } else {
                         const int slot = atomicAdd(&nlong, 1);
-                        if (slot < 64) longq[slot] = make_int4((int)(d - dst), lit_from, l, 0);
+                        if (slot < 32) longq[slot] = make_int4((int)(d - dst), lit_from, l, 0);
                     }
                     d += l;
                     d[0] = (uint8_t)off;
@@ -312,7 +329,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             }
             __syncwarp();
             const int nl = nlong;
-            if (nl > 64) {  // cannot happen: at most one long run per lane and 32 lanes
+            if (nl > 32) {  // cannot happen: a long run (> 32 bytes) only before a lane's first sequence
                 overflow = true;
                 break;
             }
