@@ -5,9 +5,10 @@ ABI in include/czgpu.h); this package is its Python binding and mirrors the
 reference compressor interface (see api.py).
 """
 from .api import (Context, CompressedField, WaveletCompressor, compress_field, compress_to_image, context,
-                  decompress_field, decompress_image, image_info, lz4_compress, lz4_decompress, params)
+                  decompress_field, decompress_image, image_info, iwt_adjoint, iwt_linear, lz4_compress,
+                  lz4_decompress, params, refit_field)
 from ._lib import CzError
 
 __all__ = ["Context", "CompressedField", "WaveletCompressor", "compress_field", "compress_to_image", "context",
-           "decompress_field", "decompress_image", "image_info", "lz4_compress", "lz4_decompress", "params",
-           "CzError"]
+           "decompress_field", "decompress_image", "image_info", "iwt_adjoint", "iwt_linear", "lz4_compress",
+           "lz4_decompress", "params", "refit_field", "CzError"]

@@ -30,7 +30,7 @@ EXPORTS = [
     "cz_lz4_bound", "cz_lz4_compress", "cz_lz4_decompress",
     "cz_field_compress", "cz_stream_copy", "cz_field_decompress", "cz_batch_compress",
     "cz_file_bytes", "cz_file_image", "cz_compress_to_image", "cz_image_info", "cz_decompress_image",
-    "cz_blocks_compress_noalloc",
+    "cz_blocks_compress_noalloc", "cz_iwt_linear", "cz_iwt_adjoint", "cz_refit",
 ]
 NOALLOC_MAX_BLOCKS = 16
 
@@ -89,5 +89,8 @@ def load():
     L.cz_image_info.argtypes = [vp, C.c_longlong, ip, ip]
     L.cz_decompress_image.argtypes = [vp, vp, C.c_longlong, C.c_int, C.c_int, vp, vp, C.c_longlong]
     L.cz_blocks_compress_noalloc.argtypes = [vp, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, vp, vp, vp]
+    L.cz_iwt_linear.argtypes = [vp, vp, C.c_longlong, C.c_int, vp, vp]
+    L.cz_iwt_adjoint.argtypes = [vp, vp, C.c_longlong, C.c_int, vp, vp]
+    L.cz_refit.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(Params), C.c_int, vp, C.POINTER(Stream)]
     _L = L
     return L

@@ -185,6 +185,44 @@ def compress_field(field, eps, wtype=1, zerobits=0, shuffle=False, encoder="lz4"
     return CompressedField(ctx, s, (nz, ny, nx), prm)
 
 
+def refit_field(field, eps, iters=30, wtype=1, zerobits=0, shuffle=False, encoder="lz4", blocks_per_chunk=1,
+                stream=None):
+    """compress_field with the retained coefficients refit by `iters` CGLS
+    steps per block (same mask, same stream layout)."""
+    import torch
+    assert field.is_cuda and field.dtype == torch.float32 and field.is_contiguous()
+    nz, ny, nx = field.shape
+    ctx = context(field.device.index or 0)
+    prm = params(eps, wtype, zerobits, shuffle, encoder, blocks_per_chunk)
+    s = Stream()
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(field.device).cuda_stream
+    ctx.check(ctx.L.cz_refit(ctx.h, C.c_void_p(field.data_ptr()), nx, ny, nz, C.byref(prm), int(iters),
+                             C.c_void_p(st), C.byref(s)))
+    return CompressedField(ctx, s, (nz, ny, nx), prm)
+
+
+def _blocks_op(name, src, wtype, stream):
+    import torch
+    assert src.is_cuda and src.dtype == torch.float32 and src.is_contiguous() and src.numel() % 32768 == 0
+    ctx = context(src.device.index or 0)
+    out = torch.empty_like(src)
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(src.device).cuda_stream
+    ctx.check(getattr(ctx.L, name)(ctx.h, C.c_void_p(src.data_ptr()), src.numel() // 32768, int(wtype),
+                                   C.c_void_p(out.data_ptr()), C.c_void_p(st)))
+    return out
+
+
+def iwt_linear(coef, wtype=1, stream=None):
+    """Inverse transform (binary32 linear map) of stacked 32^3 coefficient
+    blocks in the reference's positional layout -> stacked sample blocks."""
+    return _blocks_op("cz_iwt_linear", coef, wtype, stream)
+
+
+def iwt_adjoint(blocks, wtype=1, stream=None):
+    """Adjoint of iwt_linear: stacked sample blocks -> positional coefficients."""
+    return _blocks_op("cz_iwt_adjoint", blocks, wtype, stream)
+
+
 def decompress_field(data, offsets, shape, wtype=1, shuffle=False, encoder="lz4", blocks_per_chunk=1, out=None,
                      stream=None):
     """Decompress device chunks (uint8 tensor + int64 offsets tensor) into a

@@ -41,7 +41,7 @@ struct cz_ctx {
     std::string err;
     DevBuf fields, stage, rec_bytes, chunk_in, in_off, in_len, blk_dst, lz_off, lz_out, lz_len, out_off, out_data,
         queue, status, flag, rec_off, dec, dec_off, dec_cap, dec_len, raw_off, chunk_rec, block_chunk, block_subid,
-        tmp_field, tmp_in;
+        tmp_field, tmp_in, refit;
     void *pin = nullptr;  // small pinned host scratch
     size_t pin_cap = 0;
     // geometry of the last compressed stream
@@ -160,7 +160,7 @@ void collect(cz_ctx *c)
 // memory; fills the context's stream buffers. Returns after the total size is
 // known (one small device-to-host copy).
 int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const cz_params *p,
-                    cudaStream_t st, cz_stream *out)
+                    cudaStream_t st, cz_stream *out, int refit_iters = 0)
 {
     const int bpc = p->blocks_per_chunk;
     const long long nch_ll = (nblocks + bpc - 1) / bpc;
@@ -194,10 +194,16 @@ int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nbl
     CZ_CUDA(c, cudaMemsetAsync(c->queue.p, 0, 64, st));
     CZ_CUDA(c, cudaMemsetAsync(c->flag.p, 0, 64, st));
     const int grid = (int)std::min<long long>(nblocks, c->sms);
+    if (refit_iters > 0) CZ_TRY(grow(c, c->refit, sizeof(float) * cz_refit_scratch_floats(grid)));
     CZ_TRY(mark(c, 0, st));
-    CZ_CUDA(c, cz_launch_encode(p->wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, p->zerobits,
-                                p->shuffle ? 1 : 0, P<uint8_t>(c->stage), P<int>(c->rec_bytes),
-                                P<unsigned long long>(c->queue), grid, st));
+    if (refit_iters > 0)
+        CZ_CUDA(c, cz_launch_refit(p->wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, p->zerobits,
+                                   p->shuffle ? 1 : 0, refit_iters, P<uint8_t>(c->stage), P<int>(c->rec_bytes),
+                                   P<unsigned long long>(c->queue), P<float>(c->refit), grid, st));
+    else
+        CZ_CUDA(c, cz_launch_encode(p->wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, p->zerobits,
+                                    p->shuffle ? 1 : 0, P<uint8_t>(c->stage), P<int>(c->rec_bytes),
+                                    P<unsigned long long>(c->queue), grid, st));
     CZ_TRY(mark(c, 1, st));
     CZ_CUDA(c, cz_launch_chunk_setup(bpc, nblocks, nchunks, P<int>(c->rec_bytes), P<long long>(c->in_off),
                                      P<int>(c->in_len), bpc > 1 ? P<long long>(c->blk_dst) : nullptr,
@@ -348,7 +354,7 @@ int cz_destroy(cz_ctx *c)
 {
     if (!c) return CZ_OK;
     cudaSetDevice(c->device);
-    DevBuf *all[] = {&c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
+    DevBuf *all[] = {&c->refit, &c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
                      &c->blk_dst, &c->lz_off,  &c->lz_out,    &c->lz_len,    &c->out_off,     &c->out_data,
                      &c->queue,   &c->status,  &c->flag,      &c->rec_off,   &c->dec,         &c->dec_off,
                      &c->dec_cap, &c->dec_len, &c->raw_off,   &c->chunk_rec, &c->block_chunk, &c->block_subid,
@@ -390,6 +396,38 @@ int cz_field_compress(cz_ctx *c, const float *d_field, int nx, int ny, int nz, c
     std::vector<CzField> f(1);
     f[0] = CzField{d_field, nx, ny, nz, p->eps, 0};
     return compress_fields(c, f, nblocks, p, (cudaStream_t)stream, out);
+}
+
+int cz_refit(cz_ctx *c, const float *d_field, int nx, int ny, int nz, const cz_params *p, int iters, void *stream,
+             cz_stream *out)
+{
+    if (!c || !d_field || !out) return fail(c, CZ_E_ARG, "NULL argument");
+    if (iters < 1 || iters > 1000) return fail(c, CZ_E_ARG, "refit iterations out of range [1, 1000]");
+    CZ_TRY(check_params(c, p));
+    CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(set_device(c));
+    const long long nblocks = (long long)(nx / 32) * (ny / 32) * (nz / 32);
+    std::vector<CzField> f(1);
+    f[0] = CzField{d_field, nx, ny, nz, p->eps, 0};
+    return compress_fields(c, f, nblocks, p, (cudaStream_t)stream, out, iters);
+}
+
+int cz_iwt_linear(cz_ctx *c, const float *d_coef, long long nblocks, int wtype, float *d_blocks, void *stream)
+{
+    if (!c || !d_coef || !d_blocks || nblocks < 0) return fail(c, CZ_E_ARG, "bad arguments");
+    CZ_TRY(set_device(c));
+    const int grid = (int)std::max<long long>(1, std::min<long long>(nblocks, c->sms));
+    CZ_CUDA(c, cz_launch_iwt_linear(wtype, d_coef, d_blocks, nblocks, grid, (cudaStream_t)stream));
+    return CZ_OK;
+}
+
+int cz_iwt_adjoint(cz_ctx *c, const float *d_blocks, long long nblocks, int wtype, float *d_coef, void *stream)
+{
+    if (!c || !d_coef || !d_blocks || nblocks < 0) return fail(c, CZ_E_ARG, "bad arguments");
+    CZ_TRY(set_device(c));
+    const int grid = (int)std::max<long long>(1, std::min<long long>(nblocks, c->sms));
+    CZ_CUDA(c, cz_launch_iwt_adjoint(wtype, d_blocks, d_coef, nblocks, grid, (cudaStream_t)stream));
+    return CZ_OK;
 }
 
 int cz_stream_copy(cz_ctx *c, const cz_stream *s, uint8_t *d_data, long long *d_off, void *stream)

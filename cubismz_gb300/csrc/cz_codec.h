@@ -25,6 +25,20 @@ cudaError_t cz_launch_decode(int wtype, const CzField *fields, int nfields, long
                              const uint8_t *base, const long long *rec_off, int *status, unsigned long long *queue,
                              int grid, cudaStream_t st);
 
+// Linear inverse transform and its adjoint on stacked 32^3 blocks; block
+// coefficients in the reference's positional layout, samples x fastest
+// (cz_refit.cu).
+cudaError_t cz_launch_iwt_linear(int wtype, const float *coef, float *out, long long nblocks, int grid,
+                                 cudaStream_t st);
+cudaError_t cz_launch_iwt_adjoint(int wtype, const float *in, float *coef, long long nblocks, int grid,
+                                  cudaStream_t st);
+// Encode with the least-squares refit of the survivors (iters CGLS steps per
+// block under the plain mask); scratch holds cz_refit_scratch_floats(grid).
+size_t cz_refit_scratch_floats(int grid);
+cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long long total_blocks, int zerobits,
+                            int shuffle, int iters, uint8_t *stage, int *rec_bytes, unsigned long long *queue,
+                            float *scratch, int grid, cudaStream_t st);
+
 // LZ4 stage (cz_lz4.cu). Chunk c's input is in[in_off[c] .. in_off[c]+in_len[c]).
 // records != 0: chunks hold block records with shuffled byte planes; the
 // search skips planes 1 and 2 (copied as literals).

@@ -65,9 +65,9 @@ typedef struct {
 
 /* Compressed field held in device memory owned by the context (valid until
  * the next call on the context). data: chunk payloads back to back;
- * chunk_offsets[nchunks+1]: offsets into data; block_chunk/block_subid: the
- * chunk and index within the chunk of every block (BlockMetadata fields);
- * raw_bytes: total record bytes before the lossless stage. */
+ * chunk_offsets[nchunks+1]: offsets into data (device); nblocks: records in
+ * the stream, blocks_per_chunk of them per chunk in block order; raw_bytes:
+ * total record bytes before the lossless stage. */
 typedef struct {
     const uint8_t *data;
     long long data_bytes;
@@ -138,6 +138,27 @@ int cz_field_decompress(cz_ctx *ctx, const uint8_t *d_data, const long long *d_c
  * describes field i's chunks inside the shared stream buffers. */
 int cz_batch_compress(cz_ctx *ctx, int nfields, const float *const *d_fields, const int *dims /* 3*nfields: nx,ny,nz */,
                       const float *eps, const cz_params *p, void *stream, cz_stream *out);
+
+/* ---- least-squares refit (device buffers) ----------------------------- */
+/* The inverse transform as a linear operator and its adjoint, on nblocks
+ * stacked 32^3 blocks (block g at +g*32768). Coefficients are in the
+ * reference's positional layout (the array FullTransformEngine::fwt leaves
+ * in place, FullWaveletTransform.h:44-49); samples are x fastest.
+ * cz_iwt_linear evaluates FullTransformEngine::iwt (:51-56) in binary32
+ * with its stencils as plain linear maps (not bit-exact to the reference's
+ * binary64 stencils); cz_iwt_adjoint applies the exact transpose of that map
+ * (the transposed 1D inverse operators in reverse sweep order). No
+ * counterpart in the reference. Asynchronous on `stream`. */
+int cz_iwt_linear(cz_ctx *ctx, const float *d_coef, long long nblocks, int wtype, float *d_blocks, void *stream);
+int cz_iwt_adjoint(cz_ctx *ctx, const float *d_blocks, long long nblocks, int wtype, float *d_coef, void *stream);
+/* cz_field_compress with the retained coefficients refit: the mask is the
+ * plain path's (|c| > eps), the survivors minimise ||x - IWT(M c)||^2 per
+ * block after `iters` (1..1000) CGLS steps started from the plain
+ * survivors. Same stream layout, decoded by any reader of the plain
+ * stream. No counterpart in the reference (whose threshold keeps the
+ * forward coefficients, FullWaveletTransform.h:58-96). */
+int cz_refit(cz_ctx *ctx, const float *d_field, int nx, int ny, int nz, const cz_params *p, int iters, void *stream,
+             cz_stream *out);
 
 /* ---- allocation-free block compression (device buffers) --------------- */
 /* No counterpart in the reference. For callers that cannot call cudaMalloc

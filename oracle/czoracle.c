@@ -413,6 +413,53 @@ void czo_iwt_f64(double *block, int wtype)
 }
 
 /* ------------------------------------------------------------------------ */
+/* Adjoint of the inverse transform, from explicit matrices.                 */
+/* The inverse line operator of t1d_f64 is linear; M (n x n, row-major,      */
+/* out = M in) is built column by column from unit inputs. The 3D adjoint    */
+/* runs czo_iwt_f64's steps in reverse order with M^T on every row; the     */
+/* xy and xz swaps are their own transposes.                                 */
+/* ------------------------------------------------------------------------ */
+void czo_inv_matrix(int n, int wtype, double *M)
+{
+    double e[32];
+    for (int j = 0; j < n; ++j) {
+        for (int i = 0; i < n; ++i) e[i] = (i == j);
+        t1d_f64(e, n, wtype, 0);
+        for (int i = 0; i < n; ++i) M[i * n + j] = e[i];
+    }
+}
+static void rows_t(double *b, int z, int bs, const double *M)
+{
+    double t[32];
+    for (int y = 0; y < bs; ++y) {
+        double *r = &AT(b, z, y, 0);
+        for (int j = 0; j < bs; ++j) {
+            double acc = 0;
+            for (int i = 0; i < bs; ++i) acc += M[i * bs + j] * r[i];
+            t[j] = acc;
+        }
+        memcpy(r, t, sizeof(double) * bs);
+    }
+}
+void czo_iwt_adj_f64(double *block, int wtype)
+{
+    double M[32 * 32], t;
+    for (int bs = 32; bs >= 8; bs /= 2) {
+        czo_inv_matrix(bs, wtype, M);
+        for (int z = 0; z < bs; ++z) {
+            rows_t(block, z, bs, M);
+            for (int y = 0; y < bs; ++y)
+                for (int x = y + 1; x < bs; ++x) { t = AT(block, z, y, x); AT(block, z, y, x) = AT(block, z, x, y); AT(block, z, x, y) = t; }
+            rows_t(block, z, bs, M);
+        }
+        for (int y = 0; y < bs; ++y)
+            for (int z = 0; z < bs; ++z)
+                for (int x = z + 1; x < bs; ++x) { t = AT(block, z, y, x); AT(block, z, y, x) = AT(block, x, y, z); AT(block, x, y, z) = t; }
+        for (int z = 0; z < bs; ++z) rows_t(block, z, bs, M);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* LZ4 legacy block format.                                                  */
 /* ------------------------------------------------------------------------ */
 #define LZ_MINMATCH 4

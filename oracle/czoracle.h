@@ -53,6 +53,9 @@ int czo_block_decompress(const uint8_t *in, int nbytes, int wtype, int shuffle, 
 /* FP64 restatement of the same transform (quality oracle). */
 void czo_fwt_f64(double *block, int wtype);
 void czo_iwt_f64(double *block, int wtype);
+/* explicit inverse line operator (row-major n x n) and the adjoint of czo_iwt_f64 */
+void czo_inv_matrix(int n, int wtype, double *M);
+void czo_iwt_adj_f64(double *block, int wtype);
 
 /* LZ4 legacy block format. Decoder semantics and error conventions follow
  * LZ4_uncompress_unknownOutputSize (ThirdParty/lz4/lz4.c:802-905): returns

@@ -42,6 +42,8 @@ def lib():
         L.czo_block_decompress.argtypes = [_u8p, C.c_int, C.c_int, C.c_int, _fp]
         L.czo_fwt_f64.argtypes = [_dp, C.c_int]
         L.czo_iwt_f64.argtypes = [_dp, C.c_int]
+        L.czo_inv_matrix.argtypes = [C.c_int, C.c_int, _dp]
+        L.czo_iwt_adj_f64.argtypes = [_dp, C.c_int]
         L.czo_lz4_decompress.argtypes = [_u8p, C.c_int, _u8p, C.c_int]
         L.czo_lz4_compress.argtypes = [_u8p, C.c_int, _u8p, C.c_int]
         L.czo_lz4_bound.argtypes = [C.c_int]
@@ -76,6 +78,20 @@ def fwt_f64(block, wtype):
 def iwt_f64(block, wtype):
     b = np.ascontiguousarray(block, dtype=np.float64).copy()
     lib().czo_iwt_f64(_p(b, _dp), wtype)
+    return b
+
+
+def inv_matrix(n, wtype):
+    """The 1D inverse line operator of the FP64 restatement as an n x n matrix."""
+    M = np.zeros((n, n), np.float64)
+    lib().czo_inv_matrix(n, wtype, _p(M, _dp))
+    return M
+
+
+def iwt_adj_f64(block, wtype):
+    """Adjoint of iwt_f64 (positional coefficient layout), from explicit matrices."""
+    b = np.ascontiguousarray(block, dtype=np.float64).copy()
+    lib().czo_iwt_adj_f64(_p(b, _dp), wtype)
     return b
 
 

@@ -104,3 +104,33 @@ def test_fp64_oracle_is_close_to_binary32_path(small_field):
         assert np.max(np.abs(c32 - c64)) < 1e-5
         back = O.iwt_f64(c64, wt)
         assert np.max(np.abs(back - b)) < 1e-12
+
+
+@pytest.mark.parametrize("wtype", [1, 2, 3])
+def test_fp64_adjoint_is_the_transpose(wtype):
+    """The explicit-matrix adjoint of the FP64 inverse transform satisfies
+    <IWT c, y> = <c, IWT^T y> and, column by column, (IWT^T y)_k = <IWT e_k, y>."""
+    rng = np.random.default_rng(wtype)
+    c = rng.standard_normal((32, 32, 32))
+    y = rng.standard_normal((32, 32, 32))
+    lhs = np.vdot(O.iwt_f64(c, wtype), y)
+    rhs = np.vdot(c, O.iwt_adj_f64(y, wtype))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    adj = O.iwt_adj_f64(y, wtype).ravel()
+    for k in [0, 5, 63, 64, 300, 511, 512, 4095, 4096, 20000, 32767]:
+        e = np.zeros(32768)
+        e[k] = 1.0
+        assert abs(np.vdot(O.iwt_f64(e.reshape(32, 32, 32), wtype), y) - adj[k]) <= 1e-12 * (1 + abs(adj[k]))
+
+
+@pytest.mark.parametrize("wtype", [1, 2, 3])
+def test_fp64_inverse_matrices(wtype):
+    """The explicit 1D inverse operators invert the reference's forward line
+    transform (binary32 restatement, so to binary32 accuracy), and the FP64
+    3D inverse inverts the FP64 forward."""
+    for n in (8, 16, 32):
+        M = O.inv_matrix(n, wtype)
+        F = np.stack([O.transform1d(np.eye(n, dtype=np.float32)[j], wtype, True) for j in range(n)], axis=1)
+        assert np.abs(M @ F.astype(np.float64) - np.eye(n)).max() < 1e-5
+    x = np.random.default_rng(7).standard_normal((32, 32, 32))
+    assert np.abs(O.iwt_f64(O.fwt_f64(x, wtype), wtype) - x).max() < 1e-12
