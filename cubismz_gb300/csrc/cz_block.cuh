@@ -28,7 +28,9 @@ constexpr int kSmSeg16 = kSmSeg32 + kSeg32 * 2;             // u8 x 448
 constexpr int kSmSeg8 = kSmSeg16 + kSeg16;                  // u8 x 112
 constexpr int kSmOff = ((kSmSeg8 + kSeg8 + 15) / 16) * 16;  // int x kSegs
 constexpr int kSmWarp = ((kSmOff + 4 * (kSegs + 1) + 15) / 16) * 16;
-constexpr int kSmBytes = kSmWarp + 4 * 64;
+constexpr int kSmStage = kSmWarp + 4 * 64;                  // float x 512 per warp
+constexpr int kStagePerWarp = 512;                          // survivors of 32 runs
+constexpr int kSmBytes = kSmStage + 4 * kStagePerWarp * (kNT / 32);
 
 struct BlockRef {
     const CzField *f;
@@ -129,6 +131,7 @@ struct Shared {
     uint16_t *seg32;
     uint8_t *seg16, *seg8;
     int *off, *warp;
+    float *stage;
 };
 
 __device__ __forceinline__ Shared carve(unsigned char *smem)
@@ -141,6 +144,7 @@ __device__ __forceinline__ Shared carve(unsigned char *smem)
     s.seg8 = smem + kSmSeg8;
     s.off = reinterpret_cast<int *>(smem + kSmOff);
     s.warp = reinterpret_cast<int *>(smem + kSmWarp);
+    s.stage = reinterpret_cast<float *>(smem + kSmStage);
     return s;
 }
 
@@ -237,47 +241,93 @@ __device__ __forceinline__ int scan_segments(const Shared &s)
     return total;
 }
 
-// Survivor-order slot -> (physical position, run mask, bit within the run,
-// run offset). The 32 slots of a chunk share their level.
-struct Slot {
-    int pos;
-    unsigned mask;
-    int e;
-    int off;
-};
-__device__ __forceinline__ Slot slot_of(const Shared &s, int sidx)
+// Run r (1 .. kSegs-1) of the survivor order: its keep mask, and the
+// physical position of its bit e (the reference's order,
+// FullWaveletTransform.h:63-93: per level 8, 16, 32 the octant codes 1..7,
+// each in z,y,x order; cz_layout.cuh gives the position maps).
+__device__ __forceinline__ unsigned run_mask(const Shared &s, int r)
 {
-    Slot r;
-    if (sidx < 64) {  // coarse, z,y,x order (FullWaveletTransform.h:170-173)
-        r.pos = pidx(sidx & 3, (sidx >> 2) & 3, sidx >> 4);
-        r.mask = 0xffffffffu;
-        r.e = 0;
-        r.off = sidx;
-        return r;
+    if (r < kSegBase16) return s.seg8[r - kSegBase8];
+    if (r < kSegBase32) return s.seg16[r - kSegBase16];
+    return s.seg32[r - kSegBase32];
+}
+// Physical position of bit e of run r: base + e * stride.
+__device__ __forceinline__ void run_geom(int r, int &base, int &stride)
+{
+    if (r < kSegBase16) {  // level 8: runs of 4 along x
+        const int q = r - kSegBase8, c = (q >> 4) + 1;
+        base = pidx(4 * (c & 1), 4 * ((c >> 1) & 1) + (q & 3), 4 * (c >> 2) + ((q >> 2) & 3));
+        stride = 1;
+    } else if (r < kSegBase32) {  // level 16: runs of 8 along y
+        const int q = r - kSegBase16, c = (q >> 6) + 1;
+        base = pidx(8 * (c >> 2) + ((q >> 3) & 7), 8 * (c & 1), 8 * ((c >> 1) & 1) + (q & 7));
+        stride = SY;
+    } else {  // level 32: runs of 16 along z
+        const int q = r - kSegBase32, c = (q >> 8) + 1;
+        base = pidx(16 * ((c >> 1) & 1) + (q & 15), 16 * (c >> 2) + ((q >> 4) & 15), 16 * (c & 1));
+        stride = SZ;
     }
-    if (sidx < 512) {  // level 8: runs of 4 along x
-        const int q = sidx - 64, seg = q >> 2, e = q & 3, c = (seg >> 4) + 1;
-        r.pos = pidx(4 * (c & 1) + e, 4 * ((c >> 1) & 1) + (seg & 3), 4 * (c >> 2) + ((seg >> 2) & 3));
-        r.mask = s.seg8[seg];
-        r.e = e;
-        r.off = s.off[kSegBase8 + seg];
-        return r;
+}
+
+// Survivors of a block in stream order, 32 runs at a time per warp (one run
+// per lane; the survivors of consecutive runs are consecutive in the
+// stream). The coarse 4^3 block comes first, always kept, in z,y,x order.
+// Needs s.off from scan_segments and S, the survivor total.
+//   emit: every lane copies its run's survivors from the block into the
+//         warp's stage, then the warp hands them out in stream order,
+//         put(k, value) with k consecutive across the warp;
+//   load: the warp fetches the group's values in stream order,
+//         get(k) with k consecutive across the warp, into the stage; every
+//         lane then places its run's survivors in the block.
+template <class Put>
+__device__ __forceinline__ void emit_survivors(const Shared &s, int S, Put &&put)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *stg = s.stage + warp * kStagePerWarp;
+    if (threadIdx.x < 64) {
+        const int t = threadIdx.x;
+        put(t, s.sb[pidx(t & 3, (t >> 2) & 3, t >> 4)]);
     }
-    if (sidx < 4096) {  // level 16: runs of 8 along y
-        const int q = sidx - 512, seg = q >> 3, e = q & 7, c = (seg >> 6) + 1;
-        r.pos = pidx(8 * (c >> 2) + ((seg >> 3) & 7), 8 * (c & 1) + e, 8 * ((c >> 1) & 1) + (seg & 7));
-        r.mask = s.seg16[seg];
-        r.e = e;
-        r.off = s.off[kSegBase16 + seg];
-        return r;
+    for (int r0 = kSegBase8 + 32 * warp; r0 < kSegs; r0 += 32 * kNW) {
+        const int r = r0 + lane;
+        const unsigned m = r < kSegs ? run_mask(s, r) : 0u;
+        const int o = r < kSegs ? s.off[r] : S;
+        const int first = __shfl_sync(0xffffffffu, o, 0);
+        const int total = __shfl_sync(0xffffffffu, o + __popc(m), 31) - first;
+        if (total == 0) continue;
+        int base = 0, stride = 0;
+        if (r < kSegs) run_geom(r, base, stride);
+        int i = o - first;
+        for (unsigned mm = m; mm; mm &= mm - 1) stg[i++] = s.sb[base + (__ffs(mm) - 1) * stride];
+        __syncwarp();
+        for (int b = lane; b < total; b += 32) put(first + b, stg[b]);
+        __syncwarp();
     }
-    // level 32: runs of 16 along z
-    const int q = sidx - 4096, seg = q >> 4, e = q & 15, c = (seg >> 8) + 1;
-    r.pos = pidx(16 * ((c >> 1) & 1) + (seg & 15), 16 * (c >> 2) + ((seg >> 4) & 15), 16 * (c & 1) + e);
-    r.mask = s.seg32[seg];
-    r.e = e;
-    r.off = s.off[kSegBase32 + seg];
-    return r;
+}
+template <class Get>
+__device__ __forceinline__ void load_survivors(const Shared &s, int S, Get &&get)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *stg = s.stage + warp * kStagePerWarp;
+    if (threadIdx.x < 64) {
+        const int t = threadIdx.x;
+        s.sb[pidx(t & 3, (t >> 2) & 3, t >> 4)] = get(t);
+    }
+    for (int r0 = kSegBase8 + 32 * warp; r0 < kSegs; r0 += 32 * kNW) {
+        const int r = r0 + lane;
+        const unsigned m = r < kSegs ? run_mask(s, r) : 0u;
+        const int o = r < kSegs ? s.off[r] : S;
+        const int first = __shfl_sync(0xffffffffu, o, 0);
+        const int total = __shfl_sync(0xffffffffu, o + __popc(m), 31) - first;
+        if (total == 0) continue;
+        for (int b = lane; b < total; b += 32) stg[b] = get(first + b);
+        __syncwarp();
+        int base = 0, stride = 0;
+        if (r < kSegs) run_geom(r, base, stride);
+        int i = o - first;
+        for (unsigned mm = m; mm; mm &= mm - 1) s.sb[base + (__ffs(mm) - 1) * stride] = stg[i++];
+        __syncwarp();
+    }
 }
 
 // ------------------------------------------------------------------ decode
@@ -314,13 +364,6 @@ struct Payload {
     }
 };
 
-// Value at bit e of run `seg` (global run index): its survivor or zero.
-__device__ __forceinline__ float run_value(const Shared &s, const Payload &pl, unsigned mask, int seg, int e)
-{
-    if (!((mask >> e) & 1u)) return 0.f;
-    return pl.get(s.off[seg] + __popc(mask & ((1u << e) - 1u)));
-}
-
 // Record emission for block g once its coefficients sit in s.sb and its run
 // masks in s.seg*/s.mask32: [int32 nbytes][mask][survivors in the reference
 // order, zero-bits applied, byte planes when shuffling]
@@ -341,21 +384,17 @@ __device__ __forceinline__ void emit_record(const Shared &s, long long g, uint32
         reinterpret_cast<uint32_t *>(slot + 4)[i] = s.mask32[i];
     // ---- survivors in the reference order, zero-bits, byte planes
     uint8_t *pay = slot + 4 + kMaskBytes;
-    for (int ch = warp; ch < 1024; ch += kNW) {
-        const Slot t = slot_of(s, ch * 32 + lane);
-        if ((t.mask >> t.e) & 1u) {
-            const int k = t.off + __popc(t.mask & ((1u << t.e) - 1u));
-            const uint32_t u = __float_as_uint(s.sb[t.pos]) & zmask;
-            if (shuffle) {
-                pay[k] = (uint8_t)u;
-                pay[S + k] = (uint8_t)(u >> 8);
-                pay[2 * S + k] = (uint8_t)(u >> 16);
-                pay[3 * S + k] = (uint8_t)(u >> 24);
-            } else {
-                reinterpret_cast<uint32_t *>(pay)[k] = u;
-            }
+    emit_survivors(s, S, [&](int k, float v) {
+        const uint32_t u = __float_as_uint(v) & zmask;
+        if (shuffle) {
+            pay[k] = (uint8_t)u;
+            pay[S + k] = (uint8_t)(u >> 8);
+            pay[2 * S + k] = (uint8_t)(u >> 16);
+            pay[3 * S + k] = (uint8_t)(u >> 24);
+        } else {
+            reinterpret_cast<uint32_t *>(pay)[k] = u;
         }
-    }
+    });
 }
 
 }  // namespace cz

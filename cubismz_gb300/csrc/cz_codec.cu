@@ -164,88 +164,32 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
         if (nel - expected == 1) nel--;  // :247-250
         const bool ok = size_ok && nel == expected && !s_bad;
         if (threadIdx.x == 0) status[g] = ok ? 0 : -1;
-        Payload pl;
-        pl.p = slot + 4 + kMaskBytes;
-        pl.c = payload / 4;
-        pl.shuffle = shuffle != 0;
-        // ---- level 8 inverse (x, z, y): x lines gather coarse + level-8 runs
-        if (threadIdx.x < 64) {
-            const int y = threadIdx.x & 7, z = threadIdx.x >> 3;
-            float v[8];
-            const int chi = 1 | ((y >= 4) << 1) | ((z >= 4) << 2);
-            const int sub = ((z & 3) << 2) | (y & 3);
-            const int seghi = kSegBase8 + (chi - 1) * 16 + sub;
-            const unsigned mhi = ok ? s.seg8[seghi - kSegBase8] : 0u;
-#pragma unroll
-            for (int e = 0; e < 4; ++e) v[4 + e] = run_value(s, pl, mhi, seghi, e);
-            if (chi > 1) {
-                const int seglo = kSegBase8 + (chi - 2) * 16 + sub;
-                const unsigned mlo = ok ? s.seg8[seglo - kSegBase8] : 0u;
-#pragma unroll
-                for (int e = 0; e < 4; ++e) v[e] = run_value(s, pl, mlo, seglo, e);
-            } else {
-#pragma unroll
-                for (int e = 0; e < 4; ++e) v[e] = ok ? pl.get(e + 4 * y + 16 * z) : 0.f;
-            }
-            line_inv<8, KIND>(v);
-            st_line<8, 0>(s.sb, pidx(0, y, z), v);
+        // ---- load (FullWaveletTransform.h:99-150): zeros, then every survivor
+        // at its place, read in stream order (consecutive across each warp)
+        for (int i = threadIdx.x; i < kBS3; i += kNT) s.sb[pidx(i & 31, (i >> 5) & 31, i >> 10)] = 0.f;
+        __syncthreads();
+        if (ok) {
+            Payload pl;
+            pl.p = slot + 4 + kMaskBytes;
+            pl.c = payload / 4;
+            pl.shuffle = shuffle != 0;
+            load_survivors(s, expected, [&](int k) { return pl.get(k); });
         }
+        __syncthreads();
+        // ---- iwt: level 8 (x, z, y), level 16 (y, x, z), level 32 (z, y, x)
+        sweep<8, 0, false, KIND>(s.sb);
         __syncthreads();
         sweep<8, 2, false, KIND>(s.sb);
         __syncthreads();
         sweep<8, 1, false, KIND>(s.sb);
         __syncthreads();
-        // ---- level 16 inverse (y, x, z): y lines gather level-16 runs
-        if (threadIdx.x < 256) {
-            const int x = threadIdx.x & 15, z = threadIdx.x >> 4;
-            const int b = pidx(x, 0, z);
-            float v[16];
-            const int chi = 1 | ((z >= 8) << 1) | ((x >= 8) << 2);
-            const int sub = ((x & 7) << 3) | (z & 7);
-            const int seghi = kSegBase16 + (chi - 1) * 64 + sub;
-            const unsigned mhi = ok ? s.seg16[seghi - kSegBase16] : 0u;
-#pragma unroll
-            for (int e = 0; e < 8; ++e) v[8 + e] = run_value(s, pl, mhi, seghi, e);
-            if (chi > 1) {
-                const int seglo = kSegBase16 + (chi - 2) * 64 + sub;
-                const unsigned mlo = ok ? s.seg16[seglo - kSegBase16] : 0u;
-#pragma unroll
-                for (int e = 0; e < 8; ++e) v[e] = run_value(s, pl, mlo, seglo, e);
-            } else {
-#pragma unroll
-                for (int e = 0; e < 8; ++e) v[e] = s.sb[b + e * SY];
-            }
-            line_inv<16, KIND>(v);
-            st_line<16, 1>(s.sb, b, v);
-        }
+        sweep<16, 1, false, KIND>(s.sb);
         __syncthreads();
         sweep<16, 0, false, KIND>(s.sb);
         __syncthreads();
         sweep<16, 2, false, KIND>(s.sb);
         __syncthreads();
-        // ---- level 32 inverse (z, y, x): z lines gather level-32 runs
-        for (int l = threadIdx.x; l < 1024; l += kNT) {
-            const int x = l & 31, y = l >> 5;
-            const int b = pidx(x, y, 0);
-            float v[32];
-            const int chi = 1 | ((x >= 16) << 1) | ((y >= 16) << 2);
-            const int sub = ((y & 15) << 4) | (x & 15);
-            const int seghi = kSegBase32 + (chi - 1) * 256 + sub;
-            const unsigned mhi = ok ? s.seg32[seghi - kSegBase32] : 0u;
-#pragma unroll
-            for (int e = 0; e < 16; ++e) v[16 + e] = run_value(s, pl, mhi, seghi, e);
-            if (chi > 1) {
-                const int seglo = kSegBase32 + (chi - 2) * 256 + sub;
-                const unsigned mlo = ok ? s.seg32[seglo - kSegBase32] : 0u;
-#pragma unroll
-                for (int e = 0; e < 16; ++e) v[e] = run_value(s, pl, mlo, seglo, e);
-            } else {
-#pragma unroll
-                for (int e = 0; e < 16; ++e) v[e] = s.sb[b + e * SZ];
-            }
-            line_inv<32, KIND>(v);
-            st_line<32, 2>(s.sb, b, v);
-        }
+        sweep<32, 2, false, KIND>(s.sb);
         __syncthreads();
         sweep<32, 1, false, KIND>(s.sb);
         __syncthreads();

@@ -1,0 +1,33 @@
+"""Profiling case for the codec kernels: a 256x512x512 fp32 field (256 MiB,
+larger than L2; 60 blobs, 6 interfaces, seed 3), compressed three times with
+wtype 1, threshold 1e-3 x range, zerobits 4, shuffle and LZ4, then
+decompressed twice. Prints the per-stage device times of each call.
+
+    python -m cubismz_gb300.profile_case
+"""
+import numpy as np
+
+
+def main():
+    import torch
+    import cubismz_gb300 as cz
+    from cubismz_gb300 import synth
+    shape = (256, 512, 512)
+    field = synth.generate(shape, seed=3, blobs=60, interfaces=6)
+    eps = float(np.float32(1e-3 * (field.max() - field.min())))
+    f = torch.from_numpy(field).cuda()
+    ctx = cz.context(0)
+    ctx.set_timing(True)
+    for _ in range(3):
+        cf = cz.compress_field(f, eps, 1, 4, True, encoder="lz4")
+        print("compress stages ms (encode, lz4, assembly):", ctx.stage_times(), "raw", cf.raw_bytes,
+              "payload", cf.nbytes)
+    data, off = cf.to_device()
+    for _ in range(2):
+        cz.decompress_field(data, off, shape, 1, True, encoder="lz4")
+        print("decompress stages ms (lz4, locate, decode):", ctx.stage_times())
+    torch.cuda.synchronize()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,6 +1,8 @@
-"""The kernels' run ("segment") bookkeeping, restated from cz_codec.cu,
+"""The kernels' run ("segment") bookkeeping, restated from cz_block.cuh,
 against the reference survivor order (FullWaveletTransform.h:58-96) and the
-positional mask index (:86), over every slot of a block."""
+positional mask index (:86), over every slot of a block; and the warp
+iteration that visits the survivors of a block (for_each_survivor)."""
+import numpy as np
 
 
 def pos_of_stream(s):
@@ -28,24 +30,33 @@ def phys_of_pos(px, py, pz):
     return px, py, pz
 
 
+def run_pos(r, e):
+    """cz_block.cuh run_pos: physical (x,y,z) of bit e of global run r."""
+    if r < 113:
+        q = r - 1
+        c = (q >> 4) + 1
+        return 4 * (c & 1) + e, 4 * ((c >> 1) & 1) + (q & 3), 4 * (c >> 2) + ((q >> 2) & 3)
+    if r < 561:
+        q = r - 113
+        c = (q >> 6) + 1
+        return 8 * (c >> 2) + ((q >> 3) & 7), 8 * (c & 1) + e, 8 * ((c >> 1) & 1) + (q & 7)
+    q = r - 561
+    c = (q >> 8) + 1
+    return 16 * ((c >> 1) & 1) + (q & 15), 16 * (c >> 2) + ((q >> 4) & 15), 16 * (c & 1) + e
+
+
 def slot_of(s):
-    """cz_codec.cu slot_of: (x,y,z), run index (global), bit."""
+    """Stream slot s -> (x,y,z), global run index, bit: runs of 4 (level 8),
+    8 (level 16) and 16 (level 32) consecutive slots, positions by run_pos."""
     if s < 64:
         return (s & 3, (s >> 2) & 3, s >> 4), 0, 0
     if s < 512:
-        q = s - 64
-        seg, e = q >> 2, q & 3
-        c = (seg >> 4) + 1
-        return (4 * (c & 1) + e, 4 * ((c >> 1) & 1) + (seg & 3), 4 * (c >> 2) + ((seg >> 2) & 3)), 1 + seg, e
-    if s < 4096:
-        q = s - 512
-        seg, e = q >> 3, q & 7
-        c = (seg >> 6) + 1
-        return (8 * (c >> 2) + ((seg >> 3) & 7), 8 * (c & 1) + e, 8 * ((c >> 1) & 1) + (seg & 7)), 113 + seg, e
-    q = s - 4096
-    seg, e = q >> 4, q & 15
-    c = (seg >> 8) + 1
-    return (16 * ((c >> 1) & 1) + (seg & 15), 16 * (c >> 2) + ((seg >> 4) & 15), 16 * (c & 1) + e), 561 + seg, e
+        run, e = 1 + ((s - 64) >> 2), (s - 64) & 3
+    elif s < 4096:
+        run, e = 113 + ((s - 512) >> 3), (s - 512) & 7
+    else:
+        run, e = 561 + ((s - 4096) >> 4), (s - 4096) & 15
+    return run_pos(run, e), run, e
 
 
 def emit_runs():
@@ -106,3 +117,56 @@ def test_slots_follow_reference_order_and_runs():
             assert (run, e) > last
             last = (run, e)
     assert len(seen_pos) == 32768 and len(seen_bits) == 32768
+
+
+def run_geom(r):
+    """cz_block.cuh run_geom: bit e of run r sits at base + e * stride of the
+    padded block layout x + 33 y + 1057 z."""
+    x, y, z = run_pos(r, 0)
+    stride = 1 if r < 113 else (33 if r < 561 else 1057)
+    return x + 33 * y + 1057 * z, stride
+
+
+def emit_order(masks, off, S):
+    """cz_block.cuh emit_survivors: runs 1..2352 in groups of 32 (one per
+    lane); each lane copies its run's survivors (ascending bits) to the
+    warp's stage at o - first + i, the warp hands stage[b] out as stream
+    index first + b. Returns [(k, padded position)]."""
+    out = [(t, t % 4 + 33 * ((t >> 2) % 4) + 1057 * (t >> 4)) for t in range(64)]
+    for r0 in range(1, 2353, 32):
+        rs = [r for r in range(r0, min(r0 + 32, 2353))]
+        first = off[rs[0]]
+        total = off[rs[-1]] + bin(masks[rs[-1]]).count("1") - first
+        stage = [None] * 512
+        for r in rs:
+            base, stride = run_geom(r)
+            i = off[r] - first
+            for e in range(16):
+                if (masks[r] >> e) & 1:
+                    stage[i] = base + e * stride
+                    i += 1
+        out += [(first + b, stage[b]) for b in range(total)]
+    return out
+
+
+def test_survivor_emission_follows_the_reference_order():
+    rng = np.random.default_rng(5)
+    widths = [4] * 112 + [8] * 448 + [16] * 1792
+    for density in (0.0, 0.05, 0.3, 0.9, 1.0):
+        masks = [0]
+        for w in widths:
+            bits = rng.random(w) < density
+            masks.append(int(sum(1 << i for i in range(w) if bits[i])))
+        off = [0] * 2353
+        acc = 64
+        for r in range(1, 2353):
+            off[r] = acc
+            acc += bin(masks[r]).count("1")
+        S = acc
+        # the reference order: stream slots in order, the kept ones numbered
+        want = []
+        for slot in range(32768):
+            (x, y, z), run, e = slot_of(slot)
+            if slot < 64 or (masks[run] >> e) & 1:
+                want.append((len(want), x + 33 * y + 1057 * z))
+        assert sorted(emit_order(masks, off, S)) == want
