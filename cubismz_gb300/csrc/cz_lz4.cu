@@ -80,6 +80,21 @@ __device__ __forceinline__ void warp_copy(uint8_t *dst, const uint8_t *src, int 
     if (lane < t) dst[4 * nw + lane] = src[4 * nw + lane];
 }
 
+// n <= 32 bytes, 8 at a time with every load of a batch issued before its
+// stores (source and destination never overlap).
+__device__ __forceinline__ void copy_short(uint8_t *__restrict__ d, const uint8_t *__restrict__ s, int n)
+{
+#pragma unroll 1
+    for (int i = 0; i < n; i += 8) {
+        uint8_t b[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) b[j] = i + j < n ? __ldg(s + i + j) : (uint8_t)0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (i + j < n) d[i + j] = b[j];
+    }
+}
+
 // Bytes of a length field's continuation: n/255 bytes of 255, then n%255.
 __device__ __forceinline__ int len_bytes(int n) { return n / 255 + 1; }
 __device__ __forceinline__ void put_len_serial(uint8_t *d, int n)
@@ -192,13 +207,27 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             int end = base + kSW;
             if (end > mflimit + 1) end = mflimit + 1;
             if (end > sk.lo) end = sk.lo;
-            // ---- probe [base, end)
+            // ---- probe [base, end): the window's words are loaded up front
+            // and the next window is prefetched into L1
             bool any_match = false;
-            for (int wb = base & ~3; wb < end; wb += 128) {
+            constexpr int kSteps = (kSW + 4 + 127) / 128;
+            uint32_t wv[kSteps], wx[kSteps];
+#pragma unroll
+            for (int k = 0; k < kSteps; ++k) {
+                const int wpos = (base & ~3) + 128 * k + 4 * lane;
+                wv[k] = wpos + 4 <= L ? __ldg(reinterpret_cast<const uint32_t *>(src + wpos)) : 0u;
+                wx[k] = lane == 31 && wpos + 8 <= L ? __ldg(reinterpret_cast<const uint32_t *>(src + wpos + 4)) : 0u;
+            }
+            if (lane < kSteps && (base & ~3) + kSW + 128 * lane < L)
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(src + (base & ~3) + kSW + 128 * lane));
+#pragma unroll
+            for (int k = 0; k < kSteps; ++k) {
+                const int wb = (base & ~3) + 128 * k;
+                if (wb >= end) break;
                 const int wpos = wb + 4 * lane;
-                const uint32_t w0 = wpos + 4 <= L ? *reinterpret_cast<const uint32_t *>(src + wpos) : 0u;
+                const uint32_t w0 = wv[k];
                 uint32_t w1 = __shfl_down_sync(0xffffffffu, w0, 1);
-                if (lane == 31) w1 = wpos + 8 <= L ? *reinterpret_cast<const uint32_t *>(src + wpos + 4) : 0u;
+                if (lane == 31) w1 = wx[k];
                 uint32_t seq[4], h[4];
                 bool valid[4];
 #pragma unroll
@@ -237,7 +266,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 continue;
             }
             miss = 0;
-            // ---- walk: lane-local greedy parse of [base + 64*lane, +64)
+            // ---- walk: lane-local greedy parse of [base + kSub*lane, +kSub)
             int ns = 0, first_start = 0x7fffffff, last_start = -1, last_end = -1;
             {
                 const int w0p = base + kSub * lane;
@@ -268,9 +297,14 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             int myP = __shfl_sync(0xffffffffu, last_end, lower ? 31 - __clz(lower) : 0);
             if (!lower) myP = anchor;
             int P = has ? __shfl_sync(0xffffffffu, last_end, 31 - __clz(has)) : anchor;
-            if (__any_sync(0xffffffffu, ns > 0 && last_start < myP)) {
-                P = anchor;
-                for (int k = 0; k < 32; ++k) {
+            const unsigned bad = __ballot_sync(0xffffffffu, ns > 0 && last_start < myP);
+            if (bad) {
+                // lanes below the first failing one are exact; from there the
+                // serial rule over the lanes that have sequences
+                const int f = __ffs(bad) - 1;
+                P = __shfl_sync(0xffffffffu, myP, f);
+                for (unsigned rest = has & ~((1u << f) - 1u); rest; rest &= rest - 1u) {
+                    const int k = __ffs(rest) - 1;
                     const int ls = __shfl_sync(0xffffffffu, last_start, k);
                     const int le = __shfl_sync(0xffffffffu, last_end, k);
                     if (lane == k) myP = P;
@@ -314,7 +348,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                         d += len_bytes(l - 15);
                     }
                     if (l <= 32) {
-                        for (int b = 0; b < l; ++b) d[b] = src[lit_from + b];
+                        copy_short(d, src + lit_from, l);
                     } else {
                         const int slot = atomicAdd(&nlong, 1);
                         if (slot < 32) longq[slot] = make_int4((int)(d - dst), lit_from, l, 0);
