@@ -31,6 +31,8 @@ EXPORTS = [
     "cz_field_compress", "cz_stream_copy", "cz_field_decompress", "cz_batch_compress",
     "cz_file_bytes", "cz_file_image", "cz_compress_to_image", "cz_image_info", "cz_decompress_image",
     "cz_blocks_compress_noalloc", "cz_iwt_linear", "cz_iwt_adjoint", "cz_refit",
+    "cz_mini_bytes", "cz_mini_write", "cz_part_bytes", "cz_part_write", "cz_stream_part", "cz_tail_bytes",
+    "cz_tail_write",
 ]
 NOALLOC_MAX_BLOCKS = 16
 
@@ -92,5 +94,15 @@ def load():
     L.cz_iwt_linear.argtypes = [vp, vp, C.c_longlong, C.c_int, vp, vp]
     L.cz_iwt_adjoint.argtypes = [vp, vp, C.c_longlong, C.c_int, vp, vp]
     L.cz_refit.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(Params), C.c_int, vp, C.POINTER(Stream)]
+    L.cz_mini_bytes.restype = C.c_longlong
+    L.cz_mini_write.argtypes = [C.c_longlong, vp, C.c_longlong]
+    L.cz_part_bytes.argtypes = [C.c_longlong, C.c_int]
+    L.cz_part_bytes.restype = C.c_longlong
+    L.cz_part_write.argtypes = [vp, llp, C.c_int, vp, C.c_longlong, llp]
+    L.cz_stream_part.argtypes = [vp, C.POINTER(Stream), vp, C.c_longlong, llp]
+    L.cz_tail_bytes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(Params)]
+    L.cz_tail_bytes.restype = C.c_longlong
+    L.cz_tail_write.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, llp, ip, C.POINTER(Params), vp, C.c_longlong,
+                                llp]
     _L = L
     return L

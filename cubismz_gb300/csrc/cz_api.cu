@@ -654,6 +654,72 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
     return cz_file_image(c, &s, nx, ny, nz, p, out, cap, written);
 }
 
+// ---------------------------------------------------- several ranks, one file
+long long cz_mini_bytes(void) { return czf::mini_header_bytes(); }
+
+int cz_mini_write(long long header_offset, uint8_t *out, long long cap)
+{
+    if (!out || cap < czf::mini_header_bytes() || header_offset < czf::mini_header_bytes()) return CZ_E_ARG;
+    czf::write_mini(out, header_offset);
+    return CZ_OK;
+}
+
+long long cz_part_bytes(long long payload_bytes, int nchunks)
+{
+    if (payload_bytes < 0 || nchunks < 0) return -1;
+    return payload_bytes + 8LL * nchunks;
+}
+
+int cz_part_write(const uint8_t *payload, const long long *chunk_offsets, int nchunks, uint8_t *out, long long cap,
+                  long long *written)
+{
+    if (!chunk_offsets || !out || !written || nchunks < 1) return CZ_E_ARG;
+    if (chunk_offsets[0] != 0) return CZ_E_ARG;
+    for (int c = 0; c < nchunks; ++c)
+        if (chunk_offsets[c + 1] < chunk_offsets[c]) return CZ_E_ARG;
+    const long long bytes = chunk_offsets[nchunks];
+    if (bytes > 0 && !payload) return CZ_E_ARG;
+    if (cz_part_bytes(bytes, nchunks) > cap) return CZ_E_SPACE;
+    *written = czf::write_part(out, payload, bytes, chunk_offsets, nchunks);
+    return CZ_OK;
+}
+
+int cz_stream_part(cz_ctx *c, const cz_stream *s, uint8_t *out, long long cap, long long *written)
+{
+    if (!c || !s || !out || !written) return fail(c, CZ_E_ARG, "NULL argument");
+    CZ_TRY(set_device(c));
+    std::vector<long long> off(s->nchunks + 1);
+    CZ_CUDA(c, cudaMemcpy(off.data(), s->chunk_offsets, sizeof(long long) * (s->nchunks + 1), cudaMemcpyDeviceToHost));
+    const long long base = off[0];
+    for (auto &o : off) o -= base;
+    if (cz_part_bytes(off[s->nchunks], s->nchunks) > cap) return fail(c, CZ_E_SPACE, "part buffer too small");
+    CZ_CUDA(c, cudaMemcpy(out, s->data + base, (size_t)off[s->nchunks], cudaMemcpyDeviceToHost));
+    *written = czf::write_part(out, out, off[s->nchunks], off.data(), s->nchunks);
+    return CZ_OK;
+}
+
+long long cz_tail_bytes(int bx, int by, int bz, int nranks, const cz_params *p)
+{
+    if (!p || bx < 1 || by < 1 || bz < 1 || nranks < 1 || bz % nranks) return -1;
+    const std::string hdr = czf::header_text_sub(bx, by, bz, bx, by, bz / nranks, p->eps, p->wtype, p->encoder);
+    return czf::tail_bytes((long long)bx * by * bz, nranks, hdr);
+}
+
+int cz_tail_write(int bx, int by, int bz, int nranks, const long long *part_bytes, const int *part_chunks,
+                  const cz_params *p, uint8_t *out, long long cap, long long *written)
+{
+    if (!p || !part_bytes || !part_chunks || !out || !written) return CZ_E_ARG;
+    if (bx < 1 || by < 1 || bz < 1 || nranks < 1 || bz % nranks || p->blocks_per_chunk < 1) return CZ_E_ARG;
+    const long long bps = (long long)bx * by * (bz / nranks);
+    const long long nch = (bps + p->blocks_per_chunk - 1) / p->blocks_per_chunk;
+    for (int r = 0; r < nranks; ++r)
+        if (part_chunks[r] != nch || part_bytes[r] < 8LL * nch) return CZ_E_ARG;
+    const std::string hdr = czf::header_text_sub(bx, by, bz, bx, by, bz / nranks, p->eps, p->wtype, p->encoder);
+    if (czf::tail_bytes((long long)bx * by * bz, nranks, hdr) > cap) return CZ_E_SPACE;
+    *written = czf::write_tail(out, hdr, bx, by, bz, nranks, p->blocks_per_chunk, part_bytes, part_chunks);
+    return CZ_OK;
+}
+
 int cz_image_info(const uint8_t *img, long long size, int *dims, int *encoder)
 {
     if (!img || !dims) return CZ_E_ARG;

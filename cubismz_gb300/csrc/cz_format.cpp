@@ -36,8 +36,10 @@ const char *wavelet_name(int wtype)
 static const char *encoder_name(int enc) { return enc == 1 ? "lz4" : (enc == 2 ? "zlib" : "none"); }
 
 // The header text of SerializerIO...:495-556, formatted with the same
-// iostream defaults (the threshold is a float, the extents doubles).
-std::string header_text(int bx, int by, int bz, float threshold, int wtype, int encoder)
+// iostream defaults (the threshold is a float, the extents doubles). Blocks
+// is the whole grid, SubdomainBlocks one rank's share.
+std::string header_text_sub(int bx, int by, int bz, int sbx, int sby, int sbz, float threshold, int wtype,
+                            int encoder)
 {
     const int mx = std::max(bx, std::max(by, bz));
     const double h = (1.0 / mx) / 32;  // Grid spacing of a unit-extent grid (Grid.h:75-90)
@@ -52,13 +54,18 @@ std::string header_text(int bx, int by, int bz, float threshold, int wtype, int 
     ss << "Blocksize: " << 32 << "\n";
     ss << "Blocks: " << bx << " x " << by << " x " << bz << "\n";
     ss << "Extent: " << h * bx * 32 << " " << h * by * 32 << " " << h * bz * 32 << "\n";
-    ss << "SubdomainBlocks: " << bx << " x " << by << " x " << bz << "\n";
+    ss << "SubdomainBlocks: " << sbx << " x " << sby << " x " << sbz << "\n";
     ss << "HalfFloat: " << "no" << "\n";
     ss << "Wavelets: " << wavelet_name(wtype) << "\n";
     ss << "WaveletThreshold: " << threshold << "\n";
     ss << "Encoder: " << encoder_name(encoder) << "\n";
     ss << "==============START-BINARY-METABLOCKS==============\n";
     return ss.str();
+}
+
+std::string header_text(int bx, int by, int bz, float threshold, int wtype, int encoder)
+{
+    return header_text_sub(bx, by, bz, bx, by, bz, threshold, wtype, encoder);
 }
 
 long long mini_header_bytes() { return 8 + (long long)strlen(kOceanTitle); }
@@ -277,6 +284,61 @@ int parse_image(const uint8_t *img, long long size, Parsed &out, std::string &er
             return -1;
         }
     return 0;
+}
+
+// ------------------------------------------------ several ranks, one file
+// The writer's collective layout (SerializerIO...:371-466): rank r's data
+// (its chunks, then its LUT of chunk offsets relative to the rank's data)
+// starts at the mini header plus the exclusive scan of the ranks' data sizes
+// (MPI_Exscan, :389); the header, the ranks' BlockMetadata in rank order and
+// the HeaderLUT of every rank follow the last rank's data.
+long long write_part(uint8_t *out, const uint8_t *payload, long long payload_bytes, const long long *chunk_off,
+                     int nchunks)
+{
+    uint8_t *p = out;
+    if (payload != p) memmove(p, payload, (size_t)payload_bytes);
+    p += payload_bytes;
+    for (int c = 0; c < nchunks; ++c) put(p, (unsigned long long)chunk_off[c]);
+    return (long long)(p - out);
+}
+
+void write_mini(uint8_t *out, long long header_offset)
+{
+    uint8_t *p = out;
+    put(p, (unsigned long long)header_offset);
+    memcpy(p, kOceanTitle, strlen(kOceanTitle));
+}
+
+long long tail_bytes(long long nblocks, int nranks, const std::string &header)
+{
+    return (long long)header.size() + 20LL * nblocks + (long long)strlen(kLutTitle) + 12LL * nranks;
+}
+
+// Ranks own z-slabs of bz / nranks block layers; blocks_per_chunk records
+// per chunk in each rank's block order (ix fastest).
+long long write_tail(uint8_t *out, const std::string &header, int bx, int by, int bz, int nranks, int bpc,
+                     const long long *part_bytes, const int *part_chunks)
+{
+    uint8_t *p = out;
+    memcpy(p, header.data(), header.size());
+    p += header.size();
+    const int sbz = bz / nranks;
+    const long long bps = (long long)bx * by * sbz;
+    for (int r = 0; r < nranks; ++r)
+        for (long long l = 0; l < bps; ++l) {
+            put(p, (int)(l / bpc));
+            put(p, (int)(l % bpc));
+            put(p, (int)(l % bx));
+            put(p, (int)((l / bx) % by));
+            put(p, (int)(r * sbz + l / ((long long)bx * by)));
+        }
+    memcpy(p, kLutTitle, strlen(kLutTitle));
+    p += strlen(kLutTitle);
+    for (int r = 0; r < nranks; ++r) {
+        put(p, (unsigned long long)part_bytes[r]);
+        put(p, part_chunks[r]);
+    }
+    return (long long)(p - out);
 }
 
 }  // namespace czf

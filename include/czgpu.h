@@ -178,6 +178,26 @@ int cz_blocks_compress_noalloc(const float *d_blocks, int nblocks, float eps, in
                                uint8_t *d_records, int *d_nbytes, void *stream);
 
 /* ---- .cz files (host memory) ------------------------------------------ */
+/* Several ranks writing one file (SerializerIO...:347-466). The grid of
+ * bx x by x bz blocks is split into nranks z-slabs of bz/nranks block
+ * layers; rank r compresses its slab (a field of nx x ny x nz/nranks) and
+ * contributes its part: its chunks and the LUT of their offsets relative
+ * to the part (cz_stream_part from a device stream, cz_part_write from host
+ * chunks). Part r starts at cz_mini_bytes() plus the exclusive scan of the
+ * parts' sizes (the writer's MPI_Exscan, :389); the mini header (at 0) and
+ * the tail (header, BlockMetadata of every rank, HeaderLUT; at the end of
+ * the last part) need every rank's part size and chunk count. All host
+ * memory; no GPU work except cz_stream_part's copies. */
+long long cz_mini_bytes(void);
+int cz_mini_write(long long header_offset, uint8_t *out, long long cap);
+long long cz_part_bytes(long long payload_bytes, int nchunks);
+int cz_part_write(const uint8_t *payload, const long long *chunk_offsets /* nchunks+1, from 0 */, int nchunks,
+                  uint8_t *out, long long cap, long long *written);
+int cz_stream_part(cz_ctx *ctx, const cz_stream *s, uint8_t *out, long long cap, long long *written);
+long long cz_tail_bytes(int bx, int by, int bz, int nranks, const cz_params *p);
+int cz_tail_write(int bx, int by, int bz, int nranks, const long long *part_bytes, const int *part_chunks,
+                  const cz_params *p, uint8_t *out, long long cap, long long *written);
+
 /* Size of the .cz image for a compressed stream (header, metadata, LUT). */
 long long cz_file_bytes(cz_ctx *ctx, const cz_stream *s, int nx, int ny, int nz, const cz_params *p);
 /* Write the .cz image of `s` into host buffer out (capacity cap): the

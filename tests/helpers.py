@@ -135,3 +135,36 @@ def lz4_random_stream(rng, nseq, final_lit=12):
     z += lits
     out += lits
     return bytes(z), bytes(out)
+
+
+def parse_cz(img):
+    """A .cz image read the way the reference reader reads it
+    (Reader_WaveletCompression.h:255-560): header keys, BlockMetadata, and
+    for every subdomain its chunks as named by its LUT."""
+    hoff = int(np.frombuffer(img[:8], np.uint64)[0])
+    text_end = img.index(b"==============START-BINARY-METABLOCKS==============\n", hoff)
+    keys = {}
+    for line in img[hoff:text_end].decode().splitlines():
+        if ":" in line:
+            k, v = line.split(":", 1)
+            keys[k.strip()] = v.strip()
+    dims = tuple(int(x) for x in keys["Blocks"].split(" x "))
+    sub = tuple(int(x) for x in keys["SubdomainBlocks"].split(" x "))
+    nblocks = dims[0] * dims[1] * dims[2]
+    pos = text_end + len("==============START-BINARY-METABLOCKS==============\n")
+    meta = [tuple(int(v) for v in np.frombuffer(img[pos + 20 * i:pos + 20 * i + 20], np.int32))
+            for i in range(nblocks)]
+    pos += 20 * nblocks
+    pos += len(LUTTITLE)
+    nsub = nblocks // (sub[0] * sub[1] * sub[2])
+    base = 8 + len(OCEAN)
+    ranks = []
+    for s in range(nsub):
+        agg = int(np.frombuffer(img[pos + 12 * s:pos + 12 * s + 8], np.uint64)[0])
+        nch = int(np.frombuffer(img[pos + 12 * s + 8:pos + 12 * s + 12], np.int32)[0])
+        lut = np.frombuffer(img[base + agg - 8 * nch:base + agg], np.uint64).astype(np.int64)
+        ends = list(lut[1:]) + [agg - 8 * nch]
+        ranks.append([img[base + a:base + b] for a, b in zip(lut, ends)])
+        base += agg
+    assert base == hoff
+    return {"blocks": dims, "subdomain": sub, "meta": meta, "ranks": ranks, "keys": keys}
