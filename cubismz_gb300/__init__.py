@@ -6,9 +6,9 @@ reference compressor interface (see api.py).
 """
 from .api import (Context, CompressedField, WaveletCompressor, compress_field, compress_to_image, context,
                   decompress_field, decompress_image, image_info, iwt_adjoint, iwt_linear, lz4_compress,
-                  lz4_decompress, params, refit_field)
+                  lz4_decompress, params, Plan, refit_field)
 from ._lib import CzError
 
 __all__ = ["Context", "CompressedField", "WaveletCompressor", "compress_field", "compress_to_image", "context",
            "decompress_field", "decompress_image", "image_info", "iwt_adjoint", "iwt_linear", "lz4_compress",
-           "lz4_decompress", "params", "refit_field", "CzError"]
+           "lz4_decompress", "params", "Plan", "refit_field", "CzError"]

@@ -32,7 +32,8 @@ EXPORTS = [
     "cz_file_bytes", "cz_file_image", "cz_compress_to_image", "cz_image_info", "cz_decompress_image",
     "cz_blocks_compress_noalloc", "cz_iwt_linear", "cz_iwt_adjoint", "cz_refit",
     "cz_mini_bytes", "cz_mini_write", "cz_part_bytes", "cz_part_write", "cz_stream_part", "cz_tail_bytes",
-    "cz_tail_write",
+    "cz_tail_write", "cz_plan_create", "cz_plan_launch", "cz_plan_result", "cz_plan_info", "cz_plan_last_error",
+    "cz_plan_destroy",
 ]
 NOALLOC_MAX_BLOCKS = 16
 
@@ -100,6 +101,14 @@ def load():
     L.cz_part_bytes.restype = C.c_longlong
     L.cz_part_write.argtypes = [vp, llp, C.c_int, vp, C.c_longlong, llp]
     L.cz_stream_part.argtypes = [vp, C.POINTER(Stream), vp, C.c_longlong, llp]
+    L.cz_plan_create.argtypes = [vp, C.c_int, C.POINTER(C.c_void_p), ip, fp, C.POINTER(Params), C.c_int,
+                                 C.POINTER(C.c_void_p)]
+    L.cz_plan_launch.argtypes = [vp, vp]
+    L.cz_plan_result.argtypes = [vp, vp, C.POINTER(Stream), C.POINTER(Stream)]
+    L.cz_plan_info.argtypes = [vp, ip, fp]
+    L.cz_plan_last_error.argtypes = [vp]
+    L.cz_plan_last_error.restype = C.c_char_p
+    L.cz_plan_destroy.argtypes = [vp]
     L.cz_tail_bytes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(Params)]
     L.cz_tail_bytes.restype = C.c_longlong
     L.cz_tail_write.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, llp, ip, C.POINTER(Params), vp, C.c_longlong,

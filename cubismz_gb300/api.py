@@ -185,6 +185,70 @@ def compress_field(field, eps, wtype=1, zerobits=0, shuffle=False, encoder="lz4"
     return CompressedField(ctx, s, (nz, ny, nx), prm)
 
 
+class Plan:
+    """A batch of CUDA fields (shape (nz, ny, nx), float32, contiguous) with
+    per-field thresholds, compressed by one captured CUDA graph (one
+    persistent wavelet launch over all fields' blocks, then the LZ4 stage
+    and the stream assembly); the LZ4 launch shape is tuned on the batch
+    when `tune` is set. Field contents may change between launches."""
+
+    def __init__(self, fields, eps, wtype=1, zerobits=0, shuffle=False, encoder="lz4", tune=True):
+        import torch
+        for f in fields:
+            assert f.is_cuda and f.dtype == torch.float32 and f.is_contiguous()
+        self.fields = list(fields)
+        self.ctx = context(self.fields[0].device.index or 0)
+        n = len(self.fields)
+        ptrs = (C.c_void_p * n)(*[f.data_ptr() for f in self.fields])
+        dims = (C.c_int * (3 * n))(*[d for f in self.fields for d in (f.shape[2], f.shape[1], f.shape[0])])
+        e = (C.c_float * n)(*[float(x) for x in eps])
+        self.prm = params(0.0, wtype, zerobits, shuffle, encoder, 1)
+        self.h = C.c_void_p()
+        self.ctx.check(self.ctx.L.cz_plan_create(self.ctx.h, n, ptrs, dims, e, C.byref(self.prm), int(bool(tune)),
+                                                 C.byref(self.h)))
+        self.nblocks = [(f.shape[0] // 32) * (f.shape[1] // 32) * (f.shape[2] // 32) for f in self.fields]
+
+    def launch(self, stream=None):
+        import torch
+        st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(self.fields[0].device).cuda_stream
+        rc = self.ctx.L.cz_plan_launch(self.h, C.c_void_p(st))
+        if rc != 0:
+            raise CzError(rc, "graph launch failed")
+
+    def result(self, stream=None):
+        """The batch's stream (CompressedField over all fields' chunks)."""
+        import torch
+        st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(self.fields[0].device).cuda_stream
+        s = Stream()
+        rc = self.ctx.L.cz_plan_result(self.h, C.c_void_p(st), C.byref(s), None)
+        if rc != 0:
+            raise CzError(rc, self.ctx.L.cz_plan_last_error(self.h).decode())
+        return CompressedField(self.ctx, s, None, self.prm)
+
+    def field_chunks(self, data, offsets, i):
+        """Field i's chunks out of the batch's (data, offsets) from to_device()."""
+        b0 = sum(self.nblocks[:i])
+        o = offsets[b0:b0 + self.nblocks[i] + 1]
+        return data[int(o[0]):int(o[-1])], o - o[0]
+
+    def info(self):
+        w = C.c_int(0)
+        t = (C.c_float * 3)()
+        self.ctx.L.cz_plan_info(self.h, C.byref(w), t)
+        return {"lz4_warps_per_cta": w.value, "tune_ms": {2: t[0], 4: t[1], 8: t[2]}}
+
+    def close(self):
+        if self.h:
+            self.ctx.L.cz_plan_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def refit_field(field, eps, iters=30, wtype=1, zerobits=0, shuffle=False, encoder="lz4", blocks_per_chunk=1,
                 stream=None):
     """compress_field with the retained coefficients refit by `iters` CGLS

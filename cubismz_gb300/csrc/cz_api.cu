@@ -156,18 +156,33 @@ void collect(cz_ctx *c)
     }
 }
 
-// Runs the compress pipeline over `nfields` descriptors already in host
-// memory; fills the context's stream buffers. Returns after the total size is
-// known (one small device-to-host copy).
-int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const cz_params *p,
-                    cudaStream_t st, cz_stream *out, int refit_iters = 0)
+// The compress pipeline in three steps:
+//   prepare  grows the context's buffers for the workload and uploads the
+//            field descriptors (may allocate and copy);
+//   enqueue  every device step on `st`, no allocation, no host wait (a CUDA
+//            graph can capture it; sizes stay on the device);
+//   finish   waits for the stream, reads the totals, fills *out.
+struct Job {
+    long long nblocks = 0;
+    int nfields = 0, nchunks = 0, bpc = 1, lz_warps = 4, refit_iters = 0;
+    long long lz_slot = 0;
+    cz_params p{};
+};
+
+int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const cz_params *p, int refit_iters,
+            cudaStream_t st, Job &job)
 {
     const int bpc = p->blocks_per_chunk;
     const long long nch_ll = (nblocks + bpc - 1) / bpc;
     if (nch_ll > 0x7fffffffLL) return fail(c, CZ_E_ARG, "too many chunks");
-    const int nchunks = (int)nch_ll;
-    const long long lz_slot = (lz4_bound_ll((long long)bpc * kSlotBytes) + 15) / 16 * 16;
-
+    job.nblocks = nblocks;
+    job.nfields = (int)fields.size();
+    job.nchunks = (int)nch_ll;
+    job.bpc = bpc;
+    job.p = *p;
+    job.refit_iters = refit_iters;
+    job.lz_slot = (lz4_bound_ll((long long)bpc * kSlotBytes) + 15) / 16 * 16;
+    const int nchunks = job.nchunks;
     CZ_TRY(grow(c, c->fields, sizeof(CzField) * fields.size()));
     CZ_TRY(grow(c, c->stage, (size_t)nblocks * kSlotBytes));
     CZ_TRY(grow(c, c->rec_bytes, sizeof(int) * nblocks));
@@ -183,31 +198,41 @@ int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nbl
         CZ_TRY(grow(c, c->blk_dst, sizeof(long long) * nblocks));
         CZ_TRY(grow(c, c->chunk_in, (size_t)nchunks * bpc * kSlotBytes));
     }
-    if (p->encoder == CZ_ENCODER_LZ4) CZ_TRY(grow(c, c->lz_out, (size_t)nchunks * lz_slot));
+    if (p->encoder == CZ_ENCODER_LZ4) CZ_TRY(grow(c, c->lz_out, (size_t)nchunks * job.lz_slot));
     // the gathered stream is bounded by the lossless bound of every chunk
-    const size_t out_cap = (size_t)nchunks * (p->encoder == CZ_ENCODER_LZ4 ? lz_slot : (long long)bpc * kSlotBytes);
+    const size_t out_cap =
+        (size_t)nchunks * (p->encoder == CZ_ENCODER_LZ4 ? job.lz_slot : (long long)bpc * kSlotBytes);
     CZ_TRY(grow(c, c->out_data, out_cap));
+    const int grid = (int)std::min<long long>(nblocks, c->sms);
+    if (refit_iters > 0) CZ_TRY(grow(c, c->refit, sizeof(float) * cz_refit_scratch_floats(grid)));
     CZ_TRY(grow_pin(c, std::max<size_t>(4096, sizeof(CzField) * fields.size() + 64)));
-
     memcpy(c->pin, fields.data(), sizeof(CzField) * fields.size());
+    // finish() reuses the pinned staging only after this copy (stream order)
     CZ_CUDA(c, cudaMemcpyAsync(c->fields.p, c->pin, sizeof(CzField) * fields.size(), cudaMemcpyHostToDevice, st));
+    return CZ_OK;
+}
+
+int enqueue(cz_ctx *c, const Job &job, cudaStream_t st, bool marks)
+{
+    const cz_params *p = &job.p;
+    const long long nblocks = job.nblocks;
+    const int nchunks = job.nchunks, bpc = job.bpc;
     CZ_CUDA(c, cudaMemsetAsync(c->queue.p, 0, 64, st));
     CZ_CUDA(c, cudaMemsetAsync(c->flag.p, 0, 64, st));
     const int grid = (int)std::min<long long>(nblocks, c->sms);
-    if (refit_iters > 0) CZ_TRY(grow(c, c->refit, sizeof(float) * cz_refit_scratch_floats(grid)));
-    CZ_TRY(mark(c, 0, st));
-    if (refit_iters > 0)
-        CZ_CUDA(c, cz_launch_refit(p->wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, p->zerobits,
-                                   p->shuffle ? 1 : 0, refit_iters, P<uint8_t>(c->stage), P<int>(c->rec_bytes),
+    if (marks) CZ_TRY(mark(c, 0, st));
+    if (job.refit_iters > 0)
+        CZ_CUDA(c, cz_launch_refit(p->wtype, P<CzField>(c->fields), job.nfields, nblocks, p->zerobits,
+                                   p->shuffle ? 1 : 0, job.refit_iters, P<uint8_t>(c->stage), P<int>(c->rec_bytes),
                                    P<unsigned long long>(c->queue), P<float>(c->refit), grid, st));
     else
-        CZ_CUDA(c, cz_launch_encode(p->wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, p->zerobits,
+        CZ_CUDA(c, cz_launch_encode(p->wtype, P<CzField>(c->fields), job.nfields, nblocks, p->zerobits,
                                     p->shuffle ? 1 : 0, P<uint8_t>(c->stage), P<int>(c->rec_bytes),
                                     P<unsigned long long>(c->queue), grid, st));
-    CZ_TRY(mark(c, 1, st));
+    if (marks) CZ_TRY(mark(c, 1, st));
     CZ_CUDA(c, cz_launch_chunk_setup(bpc, nblocks, nchunks, P<int>(c->rec_bytes), P<long long>(c->in_off),
                                      P<int>(c->in_len), bpc > 1 ? P<long long>(c->blk_dst) : nullptr,
-                                     P<long long>(c->lz_off), lz_slot, st));
+                                     P<long long>(c->lz_off), job.lz_slot, st));
     const uint8_t *chunk_src = P<uint8_t>(c->stage);
     if (bpc > 1) {
         CZ_CUDA(c, cz_launch_pack_records(P<uint8_t>(c->stage), P<int>(c->rec_bytes), nblocks,
@@ -219,36 +244,55 @@ int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nbl
     const long long *gsrc_off = P<long long>(c->in_off);
     const int *glen = P<int>(c->in_len);
     if (p->encoder == CZ_ENCODER_LZ4) {
-        const int lzgrid = std::max(1, std::min((nchunks + 3) / 4, c->sms * 8));
+        const int per = job.lz_warps;
+        const int lzgrid = std::max(1, std::min((nchunks + per - 1) / per, c->sms * (32 / per)));
         CZ_CUDA(c, cz_launch_lz4_encode(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
                                         P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<int>(c->lz_len),
-                                        p->shuffle ? 1 : 0, lzgrid, st));
+                                        p->shuffle ? 1 : 0, per, lzgrid, st));
         CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len), nchunks, P<int>(c->flag), st));
         gsrc = P<uint8_t>(c->lz_out);
         gsrc_off = P<long long>(c->lz_off);
         glen = P<int>(c->lz_len);
     }
-    CZ_TRY(mark(c, 2, st));
+    if (marks) CZ_TRY(mark(c, 2, st));
     CZ_CUDA(c, cz_launch_scan(glen, nchunks, P<long long>(c->out_off), st));
     CZ_CUDA(c, cz_launch_gather(gsrc, gsrc_off, glen, nchunks, P<uint8_t>(c->out_data), P<long long>(c->out_off), st));
-    CZ_TRY(mark(c, 3, st));
+    if (marks) CZ_TRY(mark(c, 3, st));
+    return CZ_OK;
+}
+
+int finish(cz_ctx *c, const Job &job, cudaStream_t st, cz_stream *out)
+{
     long long *h = reinterpret_cast<long long *>(c->pin);
+    const int nchunks = job.nchunks;
     CZ_CUDA(c, cudaMemcpyAsync(&h[0], P<long long>(c->out_off) + nchunks, 8, cudaMemcpyDeviceToHost, st));
     CZ_CUDA(c, cudaMemcpyAsync(&h[1], P<long long>(c->raw_off) + nchunks, 8, cudaMemcpyDeviceToHost, st));
     CZ_CUDA(c, cudaMemcpyAsync(&h[2], c->flag.p, 4, cudaMemcpyDeviceToHost, st));
     CZ_CUDA(c, cudaStreamSynchronize(st));
-    collect(c);
     if (reinterpret_cast<int *>(&h[2])[0] != 0) return fail(c, CZ_E_CUDA, "LZ4 encoder output exceeded its bound");
-    c->nblocks = nblocks;
+    c->nblocks = job.nblocks;
     c->nchunks = nchunks;
-    c->bpc = bpc;
+    c->bpc = job.bpc;
     out->data = P<uint8_t>(c->out_data);
     out->data_bytes = h[0];
     out->chunk_offsets = P<long long>(c->out_off);
     out->nchunks = nchunks;
-    out->nblocks = nblocks;
+    out->nblocks = job.nblocks;
     out->raw_bytes = h[1];
     return CZ_OK;
+}
+
+// The whole pipeline for descriptors in host memory; returns after the total
+// size is known (one small device-to-host copy).
+int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const cz_params *p,
+                    cudaStream_t st, cz_stream *out, int refit_iters = 0)
+{
+    Job job;
+    CZ_TRY(prepare(c, fields, nblocks, p, refit_iters, st, job));
+    CZ_TRY(enqueue(c, job, st, true));
+    const int rc = finish(c, job, st, out);
+    collect(c);
+    return rc;
 }
 
 // Decompress pipeline for a field whose records sit in chunks of bpc
@@ -496,6 +540,148 @@ int cz_batch_compress(cz_ctx *c, int nfields, const float *const *d_fields, cons
     return CZ_OK;
 }
 
+// ------------------------------------------------------------ batch plans
+struct cz_plan {
+    cz_ctx *c = nullptr;  // private context: its buffers are sized once, so the graph's pointers stay valid
+    Job job;
+    std::vector<long long> block0;
+    std::vector<int> nb;
+    cudaStream_t st = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    float tune_ms[3] = {-1.f, -1.f, -1.f};  // LZ4 stage per candidate: 2, 4, 8 warps per CTA
+};
+
+int cz_plan_destroy(cz_plan *pl)
+{
+    if (!pl) return CZ_OK;
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    if (pl->st) cudaStreamDestroy(pl->st);
+    if (pl->c) cz_destroy(pl->c);
+    delete pl;
+    return CZ_OK;
+}
+
+int cz_plan_create(cz_ctx *c, int nfields, const float *const *d_fields, const int *dims, const float *eps,
+                   const cz_params *p, int tune, cz_plan **out)
+{
+    if (!c || nfields <= 0 || !d_fields || !dims || !eps || !out) return fail(c, CZ_E_ARG, "bad batch arguments");
+    CZ_TRY(check_params(c, p));
+    CZ_TRY(set_device(c));
+    *out = nullptr;
+    std::vector<CzField> f(nfields);
+    cz_plan *pl = new cz_plan();
+    long long total = 0;
+    for (int i = 0; i < nfields; ++i) {
+        const int rc = check_dims(c, dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]);
+        if (rc != CZ_OK || !d_fields[i]) {
+            cz_plan_destroy(pl);
+            return rc != CZ_OK ? rc : fail(c, CZ_E_ARG, "NULL field in batch");
+        }
+        f[i] = CzField{d_fields[i], dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], eps[i], total};
+        pl->block0.push_back(total);
+        pl->nb.push_back((dims[3 * i] / 32) * (dims[3 * i + 1] / 32) * (dims[3 * i + 2] / 32));
+        total += pl->nb.back();
+    }
+    cz_params q = *p;
+    q.blocks_per_chunk = 1;  // chunks never straddle fields
+    auto bail = [&](int rc, const std::string &msg) {
+        if (pl->c && !pl->c->err.empty()) c->err = pl->c->err;
+        else c->err = msg;
+        cz_plan_destroy(pl);
+        return rc;
+    };
+    int rc = cz_create(c->device, &pl->c);
+    if (rc != CZ_OK) return bail(rc, "plan context");
+    if (cudaStreamCreateWithFlags(&pl->st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(CZ_E_CUDA, "plan stream");
+    }
+    if ((rc = prepare(pl->c, f, total, &q, 0, pl->st, pl->job)) != CZ_OK) return bail(rc, "prepare");
+    // autotuner: the LZ4 stage's CTA shape (chunks per CTA), timed on this
+    // batch; every shape writes the same bytes
+    cz_stream tmp;
+    if (tune && q.encoder == CZ_ENCODER_LZ4) {
+        const int cand[3] = {2, 4, 8};
+        pl->c->timing = true;
+        float best = 1e30f;
+        for (int k = 0; k < 3; ++k) {
+            pl->job.lz_warps = cand[k];
+            float t = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {
+                if ((rc = enqueue(pl->c, pl->job, pl->st, true)) != CZ_OK) return bail(rc, "tune");
+                if ((rc = finish(pl->c, pl->job, pl->st, &tmp)) != CZ_OK) return bail(rc, "tune");
+                collect(pl->c);
+                if (rep > 0) t = std::min(t, pl->c->stage_ms[1]);
+            }
+            pl->tune_ms[k] = t;
+            if (t < best) {
+                best = t;
+                pl->job.lz_warps = cand[k];
+            }
+        }
+        // restore the winner (the loop leaves the last candidate set)
+        for (int k = 0; k < 3; ++k)
+            if (pl->tune_ms[k] == best) pl->job.lz_warps = cand[k];
+        pl->c->timing = false;
+    }
+    // one graph: memsets, wavelet kernel, chunk setup, scans, LZ4, gather
+    if (cudaStreamBeginCapture(pl->st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(CZ_E_CUDA, "stream capture");
+    }
+    rc = enqueue(pl->c, pl->job, pl->st, false);
+    const cudaError_t ec = cudaStreamEndCapture(pl->st, &pl->graph);
+    if (rc != CZ_OK || ec != cudaSuccess) {
+        cudaGetLastError();
+        return bail(rc != CZ_OK ? rc : CZ_E_CUDA, "stream capture");
+    }
+    if (cudaGraphInstantiate(&pl->exec, pl->graph, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(CZ_E_CUDA, "graph instantiation");
+    }
+    *out = pl;
+    return CZ_OK;
+}
+
+int cz_plan_launch(cz_plan *pl, void *stream)
+{
+    if (!pl || !pl->exec) return CZ_E_ARG;
+    if (cudaGraphLaunch(pl->exec, (cudaStream_t)stream) != cudaSuccess) {
+        cudaGetLastError();
+        return CZ_E_CUDA;
+    }
+    return CZ_OK;
+}
+
+int cz_plan_result(cz_plan *pl, void *stream, cz_stream *all, cz_stream *per_field)
+{
+    if (!pl || !all) return CZ_E_ARG;
+    CZ_TRY(finish(pl->c, pl->job, (cudaStream_t)stream, all));
+    if (per_field)
+        for (size_t i = 0; i < pl->nb.size(); ++i) {
+            per_field[i].data = all->data;
+            per_field[i].chunk_offsets = all->chunk_offsets + pl->block0[i];
+            per_field[i].nchunks = pl->nb[i];
+            per_field[i].nblocks = pl->nb[i];
+            per_field[i].data_bytes = -1;
+            per_field[i].raw_bytes = -1;
+        }
+    return CZ_OK;
+}
+
+int cz_plan_info(const cz_plan *pl, int *lz_warps, float *tune_ms)
+{
+    if (!pl) return CZ_E_ARG;
+    if (lz_warps) *lz_warps = pl->job.lz_warps;
+    if (tune_ms)
+        for (int k = 0; k < 3; ++k) tune_ms[k] = pl->tune_ms[k];
+    return CZ_OK;
+}
+
+const char *cz_plan_last_error(const cz_plan *pl) { return pl && pl->c ? pl->c->err.c_str() : ""; }
+
 // ---------------------------------------------------------------- per block
 int cz_block_compress(cz_ctx *c, const float *in, float eps, int wtype, int zerobits, int shuffle, uint8_t *out,
                       int *nbytes)
@@ -561,7 +747,7 @@ int cz_lz4_compress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int 
     long long *doff = reinterpret_cast<long long *>(d + meta);
     int *dlen = reinterpret_cast<int *>(d + meta + 16);
     int *dout_len = reinterpret_cast<int *>(d + meta + 20);
-    CZ_CUDA(c, cz_launch_lz4_encode(d, doff, dlen, 1, dout, doff + 1, dout_len, 0, 1, nullptr));
+    CZ_CUDA(c, cz_launch_lz4_encode(d, doff, dlen, 1, dout, doff + 1, dout_len, 0, 4, 1, nullptr));
     int n = 0;
     CZ_CUDA(c, cudaMemcpy(&n, dout_len, 4, cudaMemcpyDeviceToHost));
     if (n < 0) return fail(c, CZ_E_CUDA, "LZ4 encoder output exceeded its bound");

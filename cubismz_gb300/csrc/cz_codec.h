@@ -42,9 +42,10 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 // LZ4 stage (cz_lz4.cu). Chunk c's input is in[in_off[c] .. in_off[c]+in_len[c]).
 // records != 0: chunks hold block records with shuffled byte planes; the
 // search skips planes 1 and 2 (copied as literals).
+// warps: 2, 4 or 8 warps (chunks) per CTA; any choice gives the same bytes.
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
-                                 uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
-                                 cudaStream_t st);
+                                 uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
+                                 int grid, cudaStream_t st);
 cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, const int *out_cap, int *out_len, int grid,
                                  cudaStream_t st);

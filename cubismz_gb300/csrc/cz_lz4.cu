@@ -34,7 +34,6 @@
 
 namespace cz {
 
-constexpr int kLzWarps = 4;
 constexpr int kHashLog = 10;
 constexpr uint32_t kEmpty = 0xffffffffu;
 constexpr int kMinMatch = 4, kLastLiterals = 5, kMfLimit = 12;
@@ -162,6 +161,7 @@ __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, in
     return len < matchlimit - p ? len : matchlimit - p;
 }
 
+template <int kLzWarps>
 __global__ void __launch_bounds__(kLzWarps * 32)
 lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
                   uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records)
@@ -785,11 +785,15 @@ __global__ void gather_kernel(const uint8_t *__restrict__ src, const long long *
 using namespace cz;
 
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
-                                 uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
-                                 cudaStream_t st)
+                                 uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
+                                 int grid, cudaStream_t st)
 {
     if (nchunks <= 0) return cudaSuccess;
-    lz4_encode_kernel<<<grid, kLzWarps * 32, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records);
+    switch (warps) {
+    case 2: lz4_encode_kernel<2><<<grid, 64, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records); break;
+    case 8: lz4_encode_kernel<8><<<grid, 256, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records); break;
+    default: lz4_encode_kernel<4><<<grid, 128, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records);
+    }
     return cudaGetLastError();
 }
 

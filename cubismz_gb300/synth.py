@@ -99,3 +99,49 @@ def batch_shapes(n=96, seed=0):
     shapes = [tuple(int(e) for e in rng.choice(edges, size=3)) for _ in range(n)]
     thr = 10.0 ** rng.uniform(-5.0, -2.0, size=n)
     return shapes, thr
+
+
+def generate_torch(shape, seed=0, blobs=20, interfaces=3, noise_rms=0.05, mean=1.0, device="cuda"):
+    """The generator of `generate` evaluated with torch on `device` in
+    float32: same parameter draws (numpy, seeded), noise phases from a
+    seeded torch generator. Statistically the same fields, not the same
+    bits; for workloads too large to build on the host."""
+    import torch
+    nz, ny, nx = shape
+    rng = np.random.default_rng(seed)
+    f = torch.zeros(shape, dtype=torch.float32, device=device)
+
+    def ar(a, b):
+        return torch.arange(a, b, device=device, dtype=torch.float32)
+
+    for _ in range(blobs):
+        a = rng.uniform(0.5, 2.0)
+        sig = rng.uniform(4.0, 16.0)
+        cz, cy, cx = rng.uniform(0, nz), rng.uniform(0, ny), rng.uniform(0, nx)
+        (z0, z1), (y0, y1), (x0, x1) = _box(cz, 8 * sig, nz), _box(cy, 8 * sig, ny), _box(cx, 8 * sig, nx)
+        gz = torch.exp(-((ar(z0, z1) - cz) ** 2) / (2 * sig * sig))[:, None, None]
+        gy = torch.exp(-((ar(y0, y1) - cy) ** 2) / (2 * sig * sig))[None, :, None]
+        gx = torch.exp(-((ar(x0, x1) - cx) ** 2) / (2 * sig * sig))[None, None, :]
+        f[z0:z1, y0:y1, x0:x1] += a * (gz * gy) * gx
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    kz = torch.fft.fftfreq(nz, device=device) * nz
+    ky = torch.fft.fftfreq(ny, device=device) * ny
+    kx = torch.fft.rfftfreq(nx, device=device) * nx
+    k = torch.sqrt(kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2)
+    kmax = min(nx, ny, nz) / 2.0
+    amp = torch.where((k >= 1.0) & (k <= kmax), k.clamp(min=1.0) ** (-11.0 / 6.0), torch.zeros_like(k))
+    phase = torch.rand(k.shape, generator=g, device=device) * (2 * np.pi)
+    noise = torch.fft.irfftn(torch.polar(amp, phase), s=shape, dim=(0, 1, 2))
+    s = noise.std()
+    f += noise * (noise_rms / s) if s > 0 else noise
+    lo = min(nx, ny, nz)
+    for _ in range(interfaces):
+        cz, cy, cx = rng.uniform(0, nz), rng.uniform(0, ny), rng.uniform(0, nx)
+        r0 = rng.uniform(0.1, 0.3) * lo
+        (z0, z1), (y0, y1), (x0, x1) = _box(cz, r0 + 40, nz), _box(cy, r0 + 40, ny), _box(cx, r0 + 40, nx)
+        r = torch.sqrt((ar(z0, z1)[:, None, None] - cz) ** 2 + (ar(y0, y1)[None, :, None] - cy) ** 2 +
+                       (ar(x0, x1)[None, None, :] - cx) ** 2)
+        f[z0:z1, y0:y1, x0:x1] += 0.5 * (1.0 - torch.tanh((r - r0) / 2.0))
+    f += mean - f.mean()
+    return f.contiguous()

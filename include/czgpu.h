@@ -160,6 +160,28 @@ int cz_iwt_adjoint(cz_ctx *ctx, const float *d_blocks, long long nblocks, int wt
 int cz_refit(cz_ctx *ctx, const float *d_field, int nx, int ny, int nz, const cz_params *p, int iters, void *stream,
              cz_stream *out);
 
+/* ---- batch plans (device buffers) -------------------------------------- */
+/* A batch of fields fixed once (device pointers, extents, thresholds) and
+ * compressed many times: cz_plan_create sizes a private set of buffers,
+ * optionally tunes the launch shape of the LZ4 stage on the batch itself
+ * (tune != 0: 2, 4 or 8 chunks per CTA, timed with CUDA events; all give
+ * the same bytes), and captures the whole pipeline (one persistent wavelet
+ * launch over every field's blocks through the device work queue, chunk
+ * setup, scans, LZ4, gather) in a CUDA graph. cz_plan_launch is one graph
+ * launch with no host work; the fields' contents may change between
+ * launches. cz_plan_result waits for `stream` and describes the shared
+ * stream (all) and, if per_field is not NULL, each field's chunks as in
+ * cz_batch_compress. Records are one block per chunk. No counterpart in
+ * the reference. */
+typedef struct cz_plan cz_plan;
+int cz_plan_create(cz_ctx *ctx, int nfields, const float *const *d_fields, const int *dims /* 3*nfields */,
+                   const float *eps, const cz_params *p, int tune, cz_plan **out);
+int cz_plan_launch(cz_plan *plan, void *stream);
+int cz_plan_result(cz_plan *plan, void *stream, cz_stream *all, cz_stream *per_field);
+int cz_plan_info(const cz_plan *plan, int *lz_warps, float *tune_ms /* 3: LZ4 ms at 2, 4, 8 */);
+const char *cz_plan_last_error(const cz_plan *plan);
+int cz_plan_destroy(cz_plan *plan);
+
 /* ---- allocation-free block compression (device buffers) --------------- */
 /* No counterpart in the reference. For callers that cannot call cudaMalloc
  * (applications that hand all device memory to their own pool, pipelines
