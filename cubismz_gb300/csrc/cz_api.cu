@@ -51,6 +51,11 @@ struct cz_ctx {
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float stage_ms[3] = {0, 0, 0};
+    // the pipelined host-buffer path: copy, LZ4 and gather streams, events per slab
+    cudaStream_t s_copy = nullptr, s_gather = nullptr, s_comp = nullptr;
+    std::vector<cudaStream_t> s_lz;
+    std::vector<cudaEvent_t> ev_h2d, ev_enc, ev_lz;
+    cudaEvent_t ev_join = nullptr;
 };
 
 namespace {
@@ -407,6 +412,13 @@ int cz_destroy(cz_ctx *c)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (auto *v : {&c->ev_h2d, &c->ev_enc, &c->ev_lz})
+        for (cudaEvent_t e : *v) cudaEventDestroy(e);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    for (cudaStream_t s : c->s_lz) cudaStreamDestroy(s);
+    if (c->s_copy) cudaStreamDestroy(c->s_copy);
+    if (c->s_gather) cudaStreamDestroy(c->s_gather);
+    if (c->s_comp) cudaStreamDestroy(c->s_comp);
     if (c->pin) cudaFreeHost(c->pin);
     delete c;
     return CZ_OK;
@@ -825,6 +837,56 @@ int cz_file_image(cz_ctx *c, const cz_stream *s, int nx, int ny, int nz, const c
     return CZ_OK;
 }
 
+namespace {
+
+constexpr int kSlabs = 16;
+
+// Streams of the pipelined path: the wavelet kernels on the highest
+// priority (their CTAs are scheduled before pending LZ4 CTAs), the LZ4
+// stages on the lowest.
+int pipeline_streams(cz_ctx *c)
+{
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+        cudaGetLastError();
+        least = greatest = 0;
+    }
+    auto mk = [&](cudaStream_t &st, int prio) {
+        if (!st && cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(c, CZ_E_CUDA, "stream creation failed");
+        }
+        return CZ_OK;
+    };
+    CZ_TRY(mk(c->s_copy, 0));
+    CZ_TRY(mk(c->s_gather, 0));
+    CZ_TRY(mk(c->s_comp, greatest));
+    while ((int)c->s_lz.size() < kSlabs) {
+        cudaStream_t st = nullptr;
+        CZ_TRY(mk(st, least));
+        c->s_lz.push_back(st);
+    }
+    for (auto *v : {&c->ev_h2d, &c->ev_enc, &c->ev_lz})
+        while ((int)v->size() < kSlabs) {
+            cudaEvent_t e;
+            CZ_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            v->push_back(e);
+        }
+    if (!c->ev_join) CZ_CUDA(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    return CZ_OK;
+}
+
+}  // namespace
+
+// Host field in, .cz image in host memory out, pipelined over z-slabs of
+// whole block layers: the slabs' host-to-device copies run on a copy
+// stream; the wavelet kernel of slab i waits only for slab i's copy; slab
+// i's LZ4 stage runs on its own stream (a chunk's LZ4 is one warp's serial
+// work, so slabs overlap); the gather stream keeps the running prefix sum
+// of chunk sizes and writes each slab's chunks straight into the caller's
+// image when it is device-accessible host memory (else into the device
+// stream buffer, copied once at the end). The header, metadata and LUT are
+// written on the host after the last slab.
 int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz, const cz_params *p, void *stream,
                          uint8_t *out, long long cap, long long *written)
 {
@@ -832,12 +894,113 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
     CZ_TRY(check_params(c, p));
     CZ_TRY(check_dims(c, nx, ny, nz));
     CZ_TRY(set_device(c));
+    cudaStream_t st = (cudaStream_t)stream;
     const size_t bytes = sizeof(float) * (size_t)nx * ny * nz;
     CZ_TRY(grow(c, c->tmp_field, bytes));
-    CZ_CUDA(c, cudaMemcpyAsync(c->tmp_field.p, h_field, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
-    cz_stream s;
-    CZ_TRY(cz_field_compress(c, P<float>(c->tmp_field), nx, ny, nz, p, stream, &s));
-    return cz_file_image(c, &s, nx, ny, nz, p, out, cap, written);
+    if (p->blocks_per_chunk != 1) {  // chunks of several records: whole-field path
+        CZ_CUDA(c, cudaMemcpyAsync(c->tmp_field.p, h_field, bytes, cudaMemcpyHostToDevice, st));
+        cz_stream s;
+        CZ_TRY(cz_field_compress(c, P<float>(c->tmp_field), nx, ny, nz, p, stream, &s));
+        return cz_file_image(c, &s, nx, ny, nz, p, out, cap, written);
+    }
+    const int bx = nx / 32, by = ny / 32, bz = nz / 32;
+    const long long layer = (long long)bx * by;  // blocks (and chunks) per block layer
+    const long long nblocks = layer * bz;
+    const int nslab = std::min(bz, kSlabs);
+    const bool lz4 = p->encoder == CZ_ENCODER_LZ4;
+    CZ_TRY(pipeline_streams(c));
+    // buffers for the whole field (the slabs index into them)
+    std::vector<CzField> slabs(nslab);
+    std::vector<long long> first(nslab + 1);
+    for (int i = 0; i <= nslab; ++i) first[i] = layer * (long long)((long long)bz * i / nslab);
+    for (int i = 0; i < nslab; ++i) {
+        const long long z0 = 32 * (first[i] / layer), depth = 32 * ((first[i + 1] - first[i]) / layer);
+        slabs[i] = CzField{P<float>(c->tmp_field) + z0 * ny * nx, nx, ny, (int)depth, p->eps, 0};
+    }
+    Job job;
+    CZ_TRY(prepare(c, slabs, nblocks, p, 0, st, job));
+    CZ_TRY(grow(c, c->queue, 8 * kSlabs + 64));
+    // the payload goes straight to the image when the device can write it
+    const std::string hdr = czf::header_text(bx, by, bz, p->eps, p->wtype, p->encoder);
+    const long long mini = czf::mini_header_bytes();
+    const long long bound = (long long)job.nchunks * (lz4 ? job.lz_slot : kSlotBytes);
+    uint8_t *direct = nullptr;
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+        cap >= czf::image_bytes(bound, job.nchunks, nblocks, hdr))
+        direct = static_cast<uint8_t *>(pa.devicePointer) + mini;
+    cudaGetLastError();
+    uint8_t *dst = direct ? direct : P<uint8_t>(c->out_data);
+    CZ_CUDA(c, cudaMemsetAsync(c->queue.p, 0, 8 * kSlabs, st));
+    CZ_CUDA(c, cudaMemsetAsync(c->flag.p, 0, 64, st));
+    CZ_CUDA(c, cudaMemsetAsync(c->out_off.p, 0, 8, st));
+    CZ_CUDA(c, cudaEventRecord(c->ev_join, st));
+    CZ_CUDA(c, cudaStreamWaitEvent(c->s_gather, c->ev_join, 0));
+    CZ_CUDA(c, cudaStreamWaitEvent(c->s_copy, c->ev_join, 0));
+    CZ_CUDA(c, cudaStreamWaitEvent(c->s_comp, c->ev_join, 0));
+    cudaStream_t cs = c->s_comp;
+    for (int i = 0; i < nslab; ++i) {
+        const size_t off = (size_t)(first[i] / layer) * 32 * ny * nx, n = (size_t)(first[i + 1] - first[i]) / layer * 32 * ny * nx;
+        CZ_CUDA(c, cudaMemcpyAsync(P<float>(c->tmp_field) + off, h_field + off, n * sizeof(float),
+                                   cudaMemcpyHostToDevice, c->s_copy));
+        CZ_CUDA(c, cudaEventRecord(c->ev_h2d[i], c->s_copy));
+    }
+    unsigned long long *queues = P<unsigned long long>(c->queue);
+    for (int i = 0; i < nslab; ++i) {
+        const long long f0 = first[i];
+        const int n = (int)(first[i + 1] - f0);
+        uint8_t *stage = P<uint8_t>(c->stage) + f0 * kSlotBytes;
+        CZ_CUDA(c, cudaStreamWaitEvent(cs, c->ev_h2d[i], 0));
+        CZ_CUDA(c, cz_launch_encode(p->wtype, P<CzField>(c->fields) + i, 1, n, p->zerobits, p->shuffle ? 1 : 0, stage,
+                                    P<int>(c->rec_bytes) + f0, queues + i, std::min(n, c->sms), cs));
+        CZ_CUDA(c, cz_launch_chunk_setup(1, n, n, P<int>(c->rec_bytes) + f0, P<long long>(c->in_off) + f0,
+                                         P<int>(c->in_len) + f0, nullptr, P<long long>(c->lz_off) + f0, job.lz_slot,
+                                         cs));
+        CZ_CUDA(c, cudaEventRecord(c->ev_enc[i], cs));
+        const uint8_t *src = stage;
+        const long long *src_off = P<long long>(c->in_off) + f0;
+        const int *len = P<int>(c->in_len) + f0;
+        cudaEvent_t ready = c->ev_enc[i];
+        if (lz4) {
+            cudaStream_t ls = c->s_lz[i];
+            CZ_CUDA(c, cudaStreamWaitEvent(ls, c->ev_enc[i], 0));
+            uint8_t *lzo = P<uint8_t>(c->lz_out) + f0 * job.lz_slot;
+            const int lzgrid = std::max(1, std::min((n + 3) / 4, c->sms * 8));
+            CZ_CUDA(c, cz_launch_lz4_encode(stage, src_off, len, n, lzo, P<long long>(c->lz_off) + f0,
+                                            P<int>(c->lz_len) + f0, p->shuffle ? 1 : 0, 4, lzgrid, ls));
+            CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len) + f0, n, P<int>(c->flag), ls));
+            CZ_CUDA(c, cudaEventRecord(c->ev_lz[i], ls));
+            src = lzo;
+            src_off = P<long long>(c->lz_off) + f0;
+            len = P<int>(c->lz_len) + f0;
+            ready = c->ev_lz[i];
+        }
+        CZ_CUDA(c, cudaStreamWaitEvent(c->s_gather, ready, 0));
+        CZ_CUDA(c, cz_launch_scan_from(len, n, P<long long>(c->out_off) + f0, c->s_gather));
+        CZ_CUDA(c, cz_launch_gather(src, src_off, len, n, dst, P<long long>(c->out_off) + f0, c->s_gather));
+    }
+    CZ_CUDA(c, cudaEventRecord(c->ev_join, c->s_gather));
+    CZ_CUDA(c, cudaStreamWaitEvent(st, c->ev_join, 0));
+    // sizes and offsets back, then the host-side tail
+    std::vector<long long> off(job.nchunks + 1);
+    int flag = 0;
+    CZ_CUDA(c, cudaMemcpyAsync(off.data(), c->out_off.p, sizeof(long long) * (job.nchunks + 1), cudaMemcpyDeviceToHost,
+                               st));
+    CZ_CUDA(c, cudaMemcpyAsync(&flag, c->flag.p, 4, cudaMemcpyDeviceToHost, st));
+    CZ_CUDA(c, cudaStreamSynchronize(st));
+    if (flag != 0) return fail(c, CZ_E_CUDA, "LZ4 encoder output exceeded its bound");
+    const long long payload = off[job.nchunks];
+    const long long need = czf::image_bytes(payload, job.nchunks, nblocks, hdr);
+    if (need > cap) return fail(c, CZ_E_SPACE, "image buffer too small");
+    if (!direct) CZ_CUDA(c, cudaMemcpy(out + mini, dst, (size_t)payload, cudaMemcpyDeviceToHost));
+    std::vector<int> bc(nblocks), bsub(nblocks, 0);
+    for (long long g = 0; g < nblocks; ++g) bc[g] = (int)g;
+    *written = czf::write_image(out, out + mini, payload, off.data(), job.nchunks, bc.data(), bsub.data(), bx, by, bz,
+                                hdr);
+    c->nblocks = nblocks;
+    c->nchunks = job.nchunks;
+    c->bpc = 1;
+    return CZ_OK;
 }
 
 // ---------------------------------------------------- several ranks, one file

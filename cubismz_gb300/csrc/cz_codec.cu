@@ -33,9 +33,8 @@
 namespace cz {
 
 template <int KIND>
-__global__ void __launch_bounds__(kNT, 1)
-encode_kernel(const CzField *fields, int nfields, long long total_blocks, int zerobits, int shuffle,
-              uint8_t *stage, int *rec_bytes, unsigned long long *queue)
+__device__ __forceinline__ void encode_body(const CzField *fields, int nfields, long long total_blocks, int zerobits,
+                                            int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const Shared s = carve(smem);
@@ -121,6 +120,25 @@ encode_kernel(const CzField *fields, int nfields, long long total_blocks, int ze
         emit_record(s, g, zmask, shuffle, stage, rec_bytes);
         g = gn;
     }
+}
+
+// One CTA per SM with the whole register file.
+template <int KIND>
+__global__ void __launch_bounds__(kNT, 1)
+encode_kernel(const CzField *fields, int nfields, long long total_blocks, int zerobits, int shuffle,
+              uint8_t *stage, int *rec_bytes, unsigned long long *queue)
+{
+    encode_body<KIND>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
+}
+
+// The same with at most 120 registers per thread: leaves room on the SM for
+// a 2-warp LZ4 CTA, so that pipelined stages run side by side.
+template <int KIND>
+__global__ void __maxnreg__(120)
+encode_kernel_lean(const CzField *fields, int nfields, long long total_blocks, int zerobits, int shuffle,
+                   uint8_t *stage, int *rec_bytes, unsigned long long *queue)
+{
+    encode_body<KIND>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
 }
 
 template <int KIND>
@@ -217,12 +235,12 @@ extern "C" int cz_codec_smem_bytes(void) { return kSmBytes; }
 template <int KIND>
 static cudaError_t launch_encode(const CzField *fields, int nfields, long long total_blocks, int zerobits,
                                  int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
-                                 cudaStream_t st)
+                                 cudaStream_t st, bool lean)
 {
-    cudaError_t e = cudaFuncSetAttribute(encode_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
+    auto k = lean ? encode_kernel_lean<KIND> : encode_kernel<KIND>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
     if (e != cudaSuccess) return e;
-    encode_kernel<KIND><<<grid, kNT, kSmBytes, st>>>(fields, nfields, total_blocks, zerobits, shuffle, stage,
-                                                     rec_bytes, queue);
+    k<<<grid, kNT, kSmBytes, st>>>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
     return cudaGetLastError();
 }
 
@@ -240,12 +258,18 @@ static cudaError_t launch_decode(const CzField *fields, int nfields, long long t
 
 cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long long total_blocks, int zerobits,
                              int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
-                             cudaStream_t st)
+                             cudaStream_t st, int lean)
 {
     switch (wkind(wtype)) {
-    case 1: return launch_encode<1>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
-    case 2: return launch_encode<2>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
-    default: return launch_encode<3>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
+    case 1:
+        return launch_encode<1>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
+                                lean != 0);
+    case 2:
+        return launch_encode<2>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
+                                lean != 0);
+    default:
+        return launch_encode<3>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
+                                lean != 0);
     }
 }
 

@@ -16,9 +16,11 @@ struct CzField {
 
 extern "C" int cz_codec_smem_bytes(void);
 
+// lean: the variant capped at 120 registers per thread (room for a 2-warp
+// LZ4 CTA on the same SM); same results.
 cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long long total_blocks, int zerobits,
                              int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
-                             cudaStream_t st);
+                             cudaStream_t st, int lean = 0);
 // Record of block g at base + rec_off[g] ([int32 nbytes][record]); a
 // negative rec_off marks a block whose record is missing (status -1).
 cudaError_t cz_launch_decode(int wtype, const CzField *fields, int nfields, long long total_blocks, int shuffle,
@@ -64,6 +66,8 @@ cudaError_t cz_launch_pack_records(const uint8_t *stage, const int *rec_bytes, l
                                    const long long *blk_dst, uint8_t *chunk_in, cudaStream_t st);
 // Exclusive scan of len[0..n) into off[0..n], off[n] = total (n <= 2^31).
 cudaError_t cz_launch_scan(const int *len, int n, long long *off, cudaStream_t st);
+// The same starting from the value already in off[0] (a running total).
+cudaError_t cz_launch_scan_from(const int *len, int n, long long *off, cudaStream_t st);
 // Decode side: walks the [nbytes] headers of each decoded chunk (chunk c at
 // base + c*chunk_cap, dec_len[c] bytes) and records where every block's
 // record starts (rec_off, relative to base); -1 and status -1 on a short or

@@ -759,25 +759,42 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
     }
 }
 
+// One CTA per chunk: bytes until the destination is 16-byte aligned, then
+// 16-byte stores (each built from five 4-byte loads with funnel shifts), then
+// the tail. Wide stores matter when the destination is host memory written
+// over the CPU-GPU link.
 __global__ void gather_kernel(const uint8_t *__restrict__ src, const long long *src_off, const int *len,
                               uint8_t *__restrict__ dst, const long long *dst_off)
 {
     const int c = blockIdx.x;
     const int n = len[c];
+    if (n <= 0) return;
     const uint8_t *s = src + src_off[c];
     uint8_t *d = dst + dst_off[c];
-    // 4-byte stores once d is aligned
-    int h = (int)((4 - (reinterpret_cast<uintptr_t>(d) & 3)) & 3);
+    int h = (int)((16 - (reinterpret_cast<uintptr_t>(d) & 15)) & 15);
     if (h > n) h = n;
     if ((int)threadIdx.x < h) d[threadIdx.x] = s[threadIdx.x];
     const uint8_t *s2 = s + h;
-    uint32_t *dw = reinterpret_cast<uint32_t *>(d + h);
-    const int m = n - h, nwd = m >> 2;
+    uint4 *dw = reinterpret_cast<uint4 *>(d + h);
+    const int m = n - h, nwd = m >> 4;
     const uint32_t sa = (uint32_t)(reinterpret_cast<uintptr_t>(s2) & 3);
     const uint32_t *sw = reinterpret_cast<const uint32_t *>(s2 - sa);
-    for (int i = threadIdx.x; i < nwd; i += blockDim.x) dw[i] = sa ? __funnelshift_r(sw[i], sw[i + 1], 8 * sa) : sw[i];
-    const int t = m & 3;
-    if ((int)threadIdx.x < t) d[h + 4 * nwd + threadIdx.x] = s2[4 * nwd + threadIdx.x];
+    for (int i = threadIdx.x; i < nwd; i += blockDim.x) {
+        const uint32_t *q = sw + 4 * i;
+        const uint32_t a0 = q[0], a1 = q[1], a2 = q[2], a3 = q[3], a4 = sa ? q[4] : 0u;
+        uint4 v;
+        if (sa) {
+            v.x = __funnelshift_r(a0, a1, 8 * sa);
+            v.y = __funnelshift_r(a1, a2, 8 * sa);
+            v.z = __funnelshift_r(a2, a3, 8 * sa);
+            v.w = __funnelshift_r(a3, a4, 8 * sa);
+        } else {
+            v = make_uint4(a0, a1, a2, a3);
+        }
+        dw[i] = v;
+    }
+    const int t = m & 15;
+    if ((int)threadIdx.x < t) d[h + 16 * nwd + threadIdx.x] = s2[16 * nwd + threadIdx.x];
 }
 
 }  // namespace cz

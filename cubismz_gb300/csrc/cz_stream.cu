@@ -52,12 +52,12 @@ __global__ void pack_records_kernel(const uint8_t *__restrict__ stage, const int
 }
 
 // Single-CTA exclusive scan (chunk counts are at most a few hundred thousand).
-__global__ void __launch_bounds__(1024) scan_kernel(const int *len, int n, long long *off)
+__global__ void __launch_bounds__(1024) scan_kernel(const int *len, int n, long long *off, int carry_in)
 {
     __shared__ long long warp_sum[32];
     __shared__ long long carry;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) carry = 0;
+    if (threadIdx.x == 0) carry = carry_in ? off[0] : 0;
     __syncthreads();
     for (int base = 0; base < n; base += 1024) {
         const int i = base + threadIdx.x;
@@ -258,7 +258,13 @@ cudaError_t cz_launch_pack_records(const uint8_t *stage, const int *rec_bytes, l
 
 cudaError_t cz_launch_scan(const int *len, int n, long long *off, cudaStream_t st)
 {
-    scan_kernel<<<1, 1024, 0, st>>>(len, n, off);
+    scan_kernel<<<1, 1024, 0, st>>>(len, n, off, 0);
+    return cudaGetLastError();
+}
+
+cudaError_t cz_launch_scan_from(const int *len, int n, long long *off, cudaStream_t st)
+{
+    scan_kernel<<<1, 1024, 0, st>>>(len, n, off, 1);
     return cudaGetLastError();
 }
 
