@@ -40,6 +40,10 @@ def test_gpu_lz4_roundtrip(cz, small_field):
     toks = [rng.integers(0, 8, 7, np.uint8).tobytes() for _ in range(40)]
     samples.append(b"".join(toks[i] for i in rng.integers(0, 40, 30000)))
     samples.append(bytes(3000) + rng.integers(0, 256, 2500, np.uint8).tobytes() + bytes(9000) + b"\x01" * 70000)
+    # period 2^18: hash-table positions are kept modulo 2^18, so entries one
+    # period back alias to offset 0 and must be rejected
+    blk = rng.integers(0, 4, 1 << 18, np.uint8).tobytes()
+    samples.append(blk + blk)
     L = O.ref(4, 1, "lz4")
     for d in samples:
         z = cz.lz4_compress(d)
