@@ -33,7 +33,7 @@ EXPORTS = [
     "cz_blocks_compress_noalloc", "cz_iwt_linear", "cz_iwt_adjoint", "cz_refit",
     "cz_mini_bytes", "cz_mini_write", "cz_part_bytes", "cz_part_write", "cz_stream_part", "cz_tail_bytes",
     "cz_tail_write", "cz_plan_create", "cz_plan_launch", "cz_plan_result", "cz_plan_info", "cz_plan_last_error",
-    "cz_plan_destroy",
+    "cz_plan_destroy", "cz_field_diff", "cz_res_line", "cz_field_from_zfastest", "cz_field_to_zfastest",
 ]
 NOALLOC_MAX_BLOCKS = 16
 
@@ -109,6 +109,11 @@ def load():
     L.cz_plan_last_error.argtypes = [vp]
     L.cz_plan_last_error.restype = C.c_char_p
     L.cz_plan_destroy.argtypes = [vp]
+    L.cz_field_diff.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(Params), vp, vp, vp,
+                                C.POINTER(C.c_double)]
+    L.cz_res_line.argtypes = [C.POINTER(C.c_double), C.c_longlong, C.c_char_p, C.c_int]
+    L.cz_field_from_zfastest.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
+    L.cz_field_to_zfastest.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
     L.cz_tail_bytes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(Params)]
     L.cz_tail_bytes.restype = C.c_longlong
     L.cz_tail_write.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, llp, ip, C.POINTER(Params), vp, C.c_longlong,

@@ -287,6 +287,73 @@ def iwt_adjoint(blocks, wtype=1, stream=None):
     return _blocks_op("cz_iwt_adjoint", blocks, wtype, stream)
 
 
+def field_from_zfastest(arr, channel=0, stream=None):
+    """hdf2cz's array layout -> the codec's field: arr is a CUDA tensor of
+    shape (nx, ny, nz) or (nx, ny, nz, nch), z fastest, float32 or float64;
+    returns a float32 (nz, ny, nx) field (x fastest)."""
+    import torch
+    assert arr.is_cuda and arr.is_contiguous() and arr.dtype in (torch.float32, torch.float64)
+    nx, ny, nz = arr.shape[:3]
+    nch = arr.shape[3] if arr.dim() == 4 else 1
+    ctx = context(arr.device.index or 0)
+    out = torch.empty((nz, ny, nx), dtype=torch.float32, device=arr.device)
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(arr.device).cuda_stream
+    ctx.check(ctx.L.cz_field_from_zfastest(ctx.h, C.c_void_p(arr.data_ptr()), arr.element_size(), nch, channel, nx,
+                                           ny, nz, C.c_void_p(out.data_ptr()), C.c_void_p(st)))
+    return out
+
+
+def field_to_zfastest(field, out=None, channel=0, stream=None):
+    """The codec's (nz, ny, nx) field -> cz2hdf's layout: channel `channel`
+    of `out` (float32, shape (nx, ny, nz) or (nx, ny, nz, nch)), new if None."""
+    import torch
+    nz, ny, nx = field.shape
+    if out is None:
+        out = torch.empty((nx, ny, nz), dtype=torch.float32, device=field.device)
+    nch = out.shape[3] if out.dim() == 4 else 1
+    ctx = context(field.device.index or 0)
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(field.device).cuda_stream
+    ctx.check(ctx.L.cz_field_to_zfastest(ctx.h, C.c_void_p(field.data_ptr()), nx, ny, nz, nch, channel,
+                                         C.c_void_p(out.data_ptr()), C.c_void_p(st)))
+    return out
+
+
+def diff_field(data, offsets, shape, reference, wtype=1, shuffle=False, encoder="lz4", blocks_per_chunk=1,
+               file_bytes=None, out=None, stream=None):
+    """Decompress and compare with `reference` (CUDA float32 field of the same
+    shape) in one pass: cz2diff's statistics, and its RES line when the
+    compressed size `file_bytes` is given."""
+    import torch
+    nz, ny, nx = shape
+    dev = data.device
+    ctx = context(dev.index or 0)
+    prm = params(0.0, wtype, 0, shuffle, encoder, blocks_per_chunk)
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    stats = (C.c_double * 9)()
+    ctx.check(ctx.L.cz_field_diff(ctx.h, C.c_void_p(data.data_ptr()), C.c_void_p(offsets.data_ptr()),
+                                  offsets.numel() - 1, nx, ny, nz, C.byref(prm), C.c_void_p(reference.data_ptr()),
+                                  C.c_void_p(st), C.c_void_p(out.data_ptr() if out is not None else None), stats))
+    keys = ["e_inf", "n_inf", "e_1", "n_1", "e_2", "n_2", "min", "max", "n"]
+    res = dict(zip(keys, list(stats)))
+    if file_bytes is not None:
+        buf = C.create_string_buffer(256)
+        ctx.check(ctx.L.cz_res_line(stats, int(file_bytes), buf, 256))
+        res["res_line"] = buf.value.decode()
+    return res
+
+
+def res_line(stats, file_bytes):
+    """cz2diff's RES line from statistics (dict as returned by diff_field)."""
+    L = _lib.load()
+    keys = ["e_inf", "n_inf", "e_1", "n_1", "e_2", "n_2", "min", "max", "n"]
+    st = (C.c_double * 9)(*[float(stats[k]) for k in keys])
+    buf = C.create_string_buffer(256)
+    rc = L.cz_res_line(st, int(file_bytes), buf, 256)
+    if rc != 0:
+        raise CzError(rc, "cz_res_line failed")
+    return buf.value.decode()
+
+
 def decompress_field(data, offsets, shape, wtype=1, shuffle=False, encoder="lz4", blocks_per_chunk=1, out=None,
                      stream=None):
     """Decompress device chunks (uint8 tensor + int64 offsets tensor) into a

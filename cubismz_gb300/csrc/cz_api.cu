@@ -41,7 +41,7 @@ struct cz_ctx {
     std::string err;
     DevBuf fields, stage, rec_bytes, chunk_in, in_off, in_len, blk_dst, lz_off, lz_out, lz_len, out_off, out_data,
         queue, status, flag, rec_off, dec, dec_off, dec_cap, dec_len, raw_off, chunk_rec, block_chunk, block_subid,
-        tmp_field, tmp_in, refit;
+        tmp_field, tmp_in, refit, diff;
     void *pin = nullptr;  // small pinned host scratch
     size_t pin_cap = 0;
     // geometry of the last compressed stream
@@ -305,9 +305,11 @@ int compress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nbl
 // block -> (chunk, subid) map (files written by other writers).
 int decompress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const uint8_t *d_data,
                       const long long *d_off, int nchunks, int encoder, int wtype, int shuffle, int bpc,
-                      const int *h_block_chunk, const int *h_block_subid, int maxsub, cudaStream_t st)
+                      const int *h_block_chunk, const int *h_block_subid, int maxsub, cudaStream_t st,
+                      const float *diff_ref = nullptr, double *h_stats = nullptr)
 {
     const int per_chunk = h_block_chunk ? maxsub : bpc;
+    if (diff_ref) CZ_TRY(grow(c, c->diff, sizeof(double) * (8 * (size_t)nblocks + 8)));
     const long long dcap = ((long long)per_chunk * (4 + kMaxRecord) + 15) / 16 * 16;
     CZ_TRY(grow(c, c->fields, sizeof(CzField) * fields.size()));
     CZ_TRY(grow(c, c->in_len, sizeof(int) * nchunks));
@@ -361,13 +363,16 @@ int decompress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long n
     }
     const int grid = (int)std::min<long long>(nblocks, c->sms);
     CZ_TRY(mark(c, 2, st));
+    double *per_block = diff_ref ? P<double>(c->diff) : nullptr;
     CZ_CUDA(c, cz_launch_decode(wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, shuffle ? 1 : 0, base,
                                 P<long long>(c->rec_off), P<int>(c->status), P<unsigned long long>(c->queue), grid,
-                                st));
+                                st, diff_ref, per_block));
+    if (diff_ref) CZ_CUDA(c, cz_launch_diff_total(per_block, nblocks, per_block + 8 * nblocks, st));
     CZ_TRY(mark(c, 3, st));
     CZ_CUDA(c, cz_launch_status_reduce(P<int>(c->status), nblocks, P<int>(c->flag), st));
     int *hflag = reinterpret_cast<int *>(reinterpret_cast<char *>(c->pin) + pin_fields);
     CZ_CUDA(c, cudaMemcpyAsync(hflag, c->flag.p, 4, cudaMemcpyDeviceToHost, st));
+    if (diff_ref) CZ_CUDA(c, cudaMemcpyAsync(h_stats, per_block + 8 * nblocks, 64, cudaMemcpyDeviceToHost, st));
     CZ_CUDA(c, cudaStreamSynchronize(st));
     collect(c);
     if (*hflag != 0) return fail(c, CZ_E_CORRUPT, "malformed chunk or record in the compressed stream");
@@ -403,7 +408,7 @@ int cz_destroy(cz_ctx *c)
 {
     if (!c) return CZ_OK;
     cudaSetDevice(c->device);
-    DevBuf *all[] = {&c->refit, &c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
+    DevBuf *all[] = {&c->diff, &c->refit, &c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
                      &c->blk_dst, &c->lz_off,  &c->lz_out,    &c->lz_len,    &c->out_off,     &c->out_data,
                      &c->queue,   &c->status,  &c->flag,      &c->rec_off,   &c->dec,         &c->dec_off,
                      &c->dec_cap, &c->dec_len, &c->raw_off,   &c->chunk_rec, &c->block_chunk, &c->block_subid,
@@ -518,6 +523,73 @@ int cz_field_decompress(cz_ctx *c, const uint8_t *d_data, const long long *d_off
     f[0] = CzField{d_field, nx, ny, nz, p->eps, 0};
     return decompress_fields(c, f, nblocks, d_data, d_off, nchunks, p->encoder, p->wtype, p->shuffle, bpc, nullptr,
                              nullptr, 0, (cudaStream_t)stream);
+}
+
+int cz_field_diff(cz_ctx *c, const uint8_t *d_data, const long long *d_off, int nchunks, int nx, int ny, int nz,
+                  const cz_params *p, const float *d_ref, void *stream, float *d_field, double *stats)
+{
+    if (!c || !d_data || !d_off || !d_ref || !stats) return fail(c, CZ_E_ARG, "NULL argument");
+    CZ_TRY(check_params(c, p));
+    CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(set_device(c));
+    const long long nblocks = (long long)(nx / 32) * (ny / 32) * (nz / 32);
+    const int bpc = p->blocks_per_chunk;
+    if ((long long)nchunks != (nblocks + bpc - 1) / bpc) return fail(c, CZ_E_ARG, "chunk count does not match the field");
+    if (!d_field) {
+        CZ_TRY(grow(c, c->tmp_field, sizeof(float) * (size_t)nx * ny * nz));
+        d_field = P<float>(c->tmp_field);
+    }
+    std::vector<CzField> f(1);
+    f[0] = CzField{d_field, nx, ny, nz, p->eps, 0};
+    double t[8];
+    CZ_TRY(decompress_fields(c, f, nblocks, d_data, d_off, nchunks, p->encoder, p->wtype, p->shuffle, bpc, nullptr,
+                             nullptr, 0, (cudaStream_t)stream, d_ref, t));
+    // {e_inf, n_inf, e_1, e_2, n_1, n_2, min, max} -> the header's order
+    stats[0] = t[0];
+    stats[1] = t[1];
+    stats[2] = t[2];
+    stats[3] = t[4];
+    stats[4] = t[3];
+    stats[5] = t[5];
+    stats[6] = t[6];
+    stats[7] = t[7];
+    stats[8] = (double)nx * ny * nz;
+    return CZ_OK;
+}
+
+int cz_res_line(const double *st, long long compressed_bytes, char *buf, int len)
+{
+    if (!st || !buf || len < 1 || st[8] <= 0) return CZ_E_ARG;
+    // Tools/cz2diff.cpp:228-261
+    const double n = st[8], e_inf = st[0], n_inf = st[1], e_1 = st[2], n_1 = st[3], e_2 = st[4], n_2 = st[5];
+    const double uncompressed = sizeof(float) * n, compressed = (double)compressed_bytes;
+    const long double mse = e_2 / n;
+    const double psnr = 20 * log10((st[7] - st[6]) / (2 * sqrt(mse)));
+    const int w = snprintf(buf, (size_t)len, "RES: %12.2f %.6e %.6e %.6e %.6e %.6e %12.04f %12.04f",
+                           uncompressed / compressed, e_inf / n_inf, e_1 / n_1, e_1 / n, sqrt(e_2) / sqrt(n_2),
+                           sqrt(e_2) / n, compressed * 8. / n, psnr);
+    return w < len ? CZ_OK : CZ_E_SPACE;
+}
+
+int cz_field_from_zfastest(cz_ctx *c, const void *d_in, int bytes, int nch, int ch, int nx, int ny, int nz,
+                           float *d_field, void *stream)
+{
+    if (!c || !d_in || !d_field || (bytes != 4 && bytes != 8) || nch < 1 || ch < 0 || ch >= nch || nx < 1 || ny < 1 ||
+        nz < 1 || ny > 65535)
+        return fail(c, CZ_E_ARG, "bad layout arguments");
+    CZ_TRY(set_device(c));
+    CZ_CUDA(c, cz_launch_from_zfastest(d_in, bytes, nch, ch, nx, ny, nz, d_field, (cudaStream_t)stream));
+    return CZ_OK;
+}
+
+int cz_field_to_zfastest(cz_ctx *c, const float *d_field, int nx, int ny, int nz, int nch, int ch, float *d_out,
+                         void *stream)
+{
+    if (!c || !d_field || !d_out || nch < 1 || ch < 0 || ch >= nch || nx < 1 || ny < 1 || nz < 1 || ny > 65535)
+        return fail(c, CZ_E_ARG, "bad layout arguments");
+    CZ_TRY(set_device(c));
+    CZ_CUDA(c, cz_launch_to_zfastest(d_field, nx, ny, nz, nch, ch, d_out, (cudaStream_t)stream));
+    return CZ_OK;
 }
 
 int cz_batch_compress(cz_ctx *c, int nfields, const float *const *d_fields, const int *dims, const float *eps,

@@ -141,10 +141,72 @@ encode_kernel_lean(const CzField *fields, int nfields, long long total_blocks, i
     encode_body<KIND>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
 }
 
-template <int KIND>
+// Error statistics of a decoded block against a reference field (the
+// quantities of cz2diff, Tools/cz2diff.cpp:116-261): per block
+// {e_inf, n_inf, e_1, n_1, e_2, n_2, min, max} with e = |decoded - ref|,
+// n = |ref|. The difference is exact (two-sum), maxima are exact, the sums
+// are compensated binary32 per thread and binary64 beyond.
+struct DiffAcc {
+    float es = 0.f, ee = 0.f;  // largest error as s + e (two-sum parts)
+    float ninf = 0.f, mn = 3.4e38f, mx = -3.4e38f;
+    float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};  // e_1, e_2, n_1, n_2 (Neumaier)
+    __device__ __forceinline__ void add(int k, float x)
+    {
+        const float t = __fadd_rn(s[k], x);
+        c[k] = __fadd_rn(c[k], fabsf(s[k]) >= fabsf(x) ? __fadd_rn(__fsub_rn(s[k], t), x)
+                                                       : __fadd_rn(__fsub_rn(x, t), s[k]));
+        s[k] = t;
+    }
+    __device__ __forceinline__ void put(float f1, float f2)
+    {
+        // TwoSum(f1, -f2): d + r == f1 - f2 exactly
+        const float d = __fadd_rn(f1, -f2);
+        const float bv = __fsub_rn(d, f1);
+        const float av = __fsub_rn(d, bv);
+        const float r = __fadd_rn(__fsub_rn(f1, av), __fsub_rn(-f2, bv));
+        const float a = fabsf(d);
+        if (a > fabsf(es) || (a == fabsf(es) && fabs((double)d + r) > fabs((double)es + ee))) {
+            es = d;
+            ee = r;
+        }
+        const float n = fabsf(f2);
+        ninf = fmaxf(ninf, n);
+        mn = fminf(mn, f2);
+        mx = fmaxf(mx, f2);
+        // every term with its rounding error: |e| = a + sgn(d) r,
+        // e^2 = a*a (+ fma residual) + 2 a sgn(d) r, n^2 = n*n (+ residual)
+        const float sr = d >= 0.f ? r : -r;
+        add(0, a);
+        add(0, sr);
+        const float a2 = __fmul_rn(a, a);
+        add(1, a2);
+        add(1, __fmaf_rn(a, a, -a2));
+        add(1, __fmul_rn(2.f * a, sr));
+        add(2, n);
+        const float n2 = __fmul_rn(n, n);
+        add(3, n2);
+        add(3, __fmaf_rn(n, n, -n2));
+    }
+};
+
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int KIND, bool DIFF>
 __global__ void __launch_bounds__(kNT, 1)
 decode_kernel(const CzField *fields, int nfields, long long total_blocks, int shuffle, const uint8_t *base,
-              const long long *rec_off, int *status, unsigned long long *queue)
+              const long long *rec_off, int *status, unsigned long long *queue, const float *diff_ref,
+              double *diff_out)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const Shared s = carve(smem);
@@ -213,17 +275,68 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
         __syncthreads();
         // x lines: inverse, then straight to the field (copy_to, WaveletCompressor.h:73-82)
         float *out = const_cast<float *>(ref.f->data);
+        DiffAcc acc;
         for (int l = threadIdx.x; l < 1024; l += kNT) {
             const int y = l & 31, z = l >> 5;
             float v[32];
             ld_line<32, 0>(s.sb, pidx(0, y, z), v);
             line_inv<32, KIND>(v);
-            float4 *dst = reinterpret_cast<float4 *>(out + row_offset(ref, y, z));
+            const size_t ro = row_offset(ref, y, z);
+            float4 *dst = reinterpret_cast<float4 *>(out + ro);
 #pragma unroll
             for (int k = 0; k < 8; ++k)
                 __stcs(dst + k, make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
+            if (DIFF) {
+                const float4 *rr = reinterpret_cast<const float4 *>(diff_ref + ro);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const float4 q = __ldcs(rr + k);
+                    acc.put(v[4 * k], q.x);
+                    acc.put(v[4 * k + 1], q.y);
+                    acc.put(v[4 * k + 2], q.z);
+                    acc.put(v[4 * k + 3], q.w);
+                }
+            }
+        }
+        if (DIFF) {
+            // block totals in binary64: maxima exact, sums of the compensated partials
+            __shared__ double red[kNW][8];
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            double t[8];
+            t[0] = warp_max(fabs((double)acc.es + acc.ee));
+            t[1] = warp_max(acc.ninf);
+            t[6] = -warp_max(-(double)acc.mn);
+            t[7] = warp_max(acc.mx);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) t[2 + k] = warp_sum((double)acc.s[k] + (double)acc.c[k]);
+            if (lane == 0)
+                for (int k = 0; k < 8; ++k) red[warp][k] = t[k];
+            __syncthreads();
+            if (threadIdx.x < 8) {
+                const int k = threadIdx.x;
+                double r = red[0][k];
+                for (int w = 1; w < kNW; ++w) {
+                    const double x = red[w][k];
+                    r = (k == 0 || k == 1 || k == 7) ? fmax(r, x) : (k == 6 ? fmin(r, x) : r + x);
+                }
+                // e_1 n_1 e_2 n_2 order of the record: {e_inf, n_inf, e_1, e_2, n_1, n_2, min, max}
+                diff_out[g * 8 + k] = r;
+            }
         }
     }
+}
+
+// Totals over blocks, in block order: {e_inf, n_inf, e_1, e_2, n_1, n_2, min, max}.
+__global__ void diff_total_kernel(const double *per_block, long long nblocks, double *total)
+{
+    const int k = threadIdx.x;
+    if (k >= 8) return;
+    double r = per_block[k];
+    for (long long g = 1; g < nblocks; ++g) {
+        const double x = per_block[g * 8 + k];
+        r = (k == 0 || k == 1 || k == 7) ? fmax(r, x) : (k == 6 ? fmin(r, x) : r + x);
+    }
+    total[k] = r;
 }
 
 }  // namespace cz
@@ -247,12 +360,14 @@ static cudaError_t launch_encode(const CzField *fields, int nfields, long long t
 template <int KIND>
 static cudaError_t launch_decode(const CzField *fields, int nfields, long long total_blocks, int shuffle,
                                  const uint8_t *base, const long long *rec_off, int *status,
-                                 unsigned long long *queue, int grid, cudaStream_t st)
+                                 unsigned long long *queue, int grid, cudaStream_t st, const float *diff_ref,
+                                 double *diff_out)
 {
-    cudaError_t e = cudaFuncSetAttribute(decode_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
+    auto k = diff_ref ? decode_kernel<KIND, true> : decode_kernel<KIND, false>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
     if (e != cudaSuccess) return e;
-    decode_kernel<KIND><<<grid, kNT, kSmBytes, st>>>(fields, nfields, total_blocks, shuffle, base, rec_off, status,
-                                                     queue);
+    k<<<grid, kNT, kSmBytes, st>>>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, diff_ref,
+                                   diff_out);
     return cudaGetLastError();
 }
 
@@ -275,11 +390,23 @@ cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long
 
 cudaError_t cz_launch_decode(int wtype, const CzField *fields, int nfields, long long total_blocks, int shuffle,
                              const uint8_t *base, const long long *rec_off, int *status, unsigned long long *queue,
-                             int grid, cudaStream_t st)
+                             int grid, cudaStream_t st, const float *diff_ref, double *diff_out)
 {
     switch (wkind(wtype)) {
-    case 1: return launch_decode<1>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st);
-    case 2: return launch_decode<2>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st);
-    default: return launch_decode<3>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st);
+    case 1:
+        return launch_decode<1>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st,
+                                diff_ref, diff_out);
+    case 2:
+        return launch_decode<2>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st,
+                                diff_ref, diff_out);
+    default:
+        return launch_decode<3>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st,
+                                diff_ref, diff_out);
     }
+}
+
+cudaError_t cz_launch_diff_total(const double *per_block, long long nblocks, double *total, cudaStream_t st)
+{
+    diff_total_kernel<<<1, 32, 0, st>>>(per_block, nblocks, total);
+    return cudaGetLastError();
 }

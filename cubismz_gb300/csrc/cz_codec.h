@@ -23,9 +23,12 @@ cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long
                              cudaStream_t st, int lean = 0);
 // Record of block g at base + rec_off[g] ([int32 nbytes][record]); a
 // negative rec_off marks a block whose record is missing (status -1).
+// diff_ref (optional, a field of the same geometry as fields[0]): per-block
+// error statistics into diff_out[8*g] (cz2diff's quantities).
 cudaError_t cz_launch_decode(int wtype, const CzField *fields, int nfields, long long total_blocks, int shuffle,
                              const uint8_t *base, const long long *rec_off, int *status, unsigned long long *queue,
-                             int grid, cudaStream_t st);
+                             int grid, cudaStream_t st, const float *diff_ref = nullptr, double *diff_out = nullptr);
+cudaError_t cz_launch_diff_total(const double *per_block, long long nblocks, double *total, cudaStream_t st);
 
 // Linear inverse transform and its adjoint on stacked 32^3 blocks; block
 // coefficients in the reference's positional layout, samples x fastest
@@ -85,3 +88,10 @@ cudaError_t cz_launch_map_blocks(long long nblocks, int nchunks, int maxsub, con
 cudaError_t cz_launch_status_reduce(const int *status, long long n, int *flag, cudaStream_t st);
 cudaError_t cz_launch_neg_reduce(const int *v, int n, int *flag, cudaStream_t st);
 cudaError_t cz_launch_rebase(long long *off, int n, long long base, cudaStream_t st);
+
+// Layout of the reference's HDF5 tools (cz_ingest.cu): z-fastest arrays with
+// interleaved channels <-> the x-fastest field. bytes: 4 (float) or 8 (double).
+cudaError_t cz_launch_from_zfastest(const void *in, int bytes, int nch, int ch, int nx, int ny, int nz, float *out,
+                                    cudaStream_t st);
+cudaError_t cz_launch_to_zfastest(const float *in, int nx, int ny, int nz, int nch, int ch, float *out,
+                                  cudaStream_t st);

@@ -133,6 +133,33 @@ int cz_stream_copy(cz_ctx *ctx, const cz_stream *s, uint8_t *d_data, long long *
 int cz_field_decompress(cz_ctx *ctx, const uint8_t *d_data, const long long *d_chunk_offsets, int nchunks, int nx,
                         int ny, int nz, const cz_params *p, void *stream, float *d_field);
 
+/* cz_field_decompress fused with cz2diff's error norms against a reference
+ * field d_ref of the same extents (Tools/cz2diff.cpp:116-261): stats =
+ * {e_inf, n_inf, e_1, n_1, e_2, n_2, min(ref), max(ref), n} with
+ * e = |decoded - ref|, n = |ref| (e_2 and n_2 are sums of squares). The
+ * differences and maxima are exact; sums are compensated per thread and
+ * binary64 beyond (the reference sums serially in binary64). d_field may be
+ * NULL (decode into context scratch). */
+int cz_field_diff(cz_ctx *ctx, const uint8_t *d_data, const long long *d_chunk_offsets, int nchunks, int nx, int ny,
+                  int nz, const cz_params *p, const float *d_ref, void *stream, float *d_field, double *stats);
+/* cz2diff's RES line from those statistics and the compressed size
+ * (CR, rel(e_inf), rel(e_1), mean(e_1), rel(e_2), mean(e_2), BPS, PSNR with
+ * PSNR = 20 log10((max-min) / (2 sqrt(mse)))), same format. Host only. */
+int cz_res_line(const double *stats, long long compressed_bytes, char *buf, int len);
+
+/* The array layout of the reference's HDF5 tools: hdf2cz reads value
+ * (gx,gy,gz) from in[ch + nch*(gz + nz*(gy + ny*gx))], z fastest, nch
+ * interleaved channels (Tools/Test_IO_Compressed.h:192-217); cz2hdf writes
+ * decoded blocks back in that order (Tools/cz2hdf.cpp:235-253). The codec's
+ * field is x fastest, d_field[gz][gy][gx]. cz_field_from_zfastest takes
+ * float (bytes = 4) or double (bytes = 8, rounded to nearest float) input;
+ * cz_field_to_zfastest writes channel ch of a float array. Device buffers,
+ * asynchronous on `stream`; ny <= 65535. */
+int cz_field_from_zfastest(cz_ctx *ctx, const void *d_in, int bytes, int nch, int ch, int nx, int ny, int nz,
+                           float *d_field, void *stream);
+int cz_field_to_zfastest(cz_ctx *ctx, const float *d_field, int nx, int ny, int nz, int nch, int ch, float *d_out,
+                         void *stream);
+
 /* Many fields of uneven extents and thresholds in one persistent launch
  * (device work queue). eps[i] per field; p->eps is ignored. out[i]
  * describes field i's chunks inside the shared stream buffers. */

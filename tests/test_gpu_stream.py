@@ -70,3 +70,25 @@ def test_large_field_properties(cz):
     full = O.field_decompress(rd, ro, field.shape, 1, 1, 0, 1, 0)
     assert np.array_equal(dec.cpu().numpy(), full)
     assert np.isfinite(full).all()
+
+
+def test_fused_decode_and_error_norms(cz, small_field):
+    """diff_field decodes and computes cz2diff's statistics in one pass:
+    maxima and range exact, sums to 1e-12 of binary64, same RES line."""
+    import torch
+    from tests.test_res import stats_f64
+    f = torch.from_numpy(small_field).cuda()
+    eps = float(np.float32(1e-3 * (small_field.max() - small_field.min())))
+    cf = cz.compress_field(f, eps, 1, 4, True, encoder="lz4")
+    data, off = cf.to_device()
+    out = torch.empty_like(f)
+    got = cz.diff_field(data, off, small_field.shape, f, 1, True, encoder="lz4", file_bytes=cf.nbytes, out=out)
+    dec = out.cpu().numpy()
+    raw, roff = O.field_compress(small_field, eps, 1, 4, 1, 0, 1)
+    assert np.array_equal(dec, O.field_decompress(raw, roff, small_field.shape, 1, 1))
+    want = stats_f64(small_field, dec)
+    for k in ("e_inf", "n_inf", "min", "max", "n"):
+        assert got[k] == want[k], k
+    for k in ("e_1", "n_1", "e_2", "n_2"):
+        assert abs(got[k] - want[k]) <= 1e-12 * abs(want[k]), k
+    assert got["res_line"] == cz.res_line(want, cf.nbytes)
