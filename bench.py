@@ -231,6 +231,57 @@ def refit_report(cz, dev):
             "refit_compress_gbs": field.nbytes / refit_s / 1e9}
 
 
+def run_stress(args):
+    """Five 1024^3 fields (density, three velocity components, pressure;
+    ~20 GiB) from independent seeds, threshold 1e-3 x range, zero-bits 4,
+    shuffle, LZ4: compress then decompress, refit disabled and enabled
+    (same mask, so the same record bytes before LZ4)."""
+    import torch
+    import cubismz_gb300 as cz
+    from cubismz_gb300 import synth
+    dev = torch.device("cuda", 0)
+    names = ["density", "velocity_x", "velocity_y", "velocity_z", "pressure"]
+    n = 1024
+    fields = [synth.generate_torch((n, n, n), seed=5000 + i, blobs=400, interfaces=20,
+                                   velocity=name.startswith("velocity"), device=dev)
+              for i, name in enumerate(names)]
+    out = {"fields": names, "shape": [n, n, n], "total_bytes": sum(f.numel() * 4 for f in fields), "per_field": []}
+    dec = torch.empty_like(fields[0])
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    stream = torch.cuda.current_stream(dev)
+    tot_c = tot_d = 0.0
+    for name, f in zip(names, fields):
+        rng_ = float(f.max() - f.min())
+        eps = float(np.float32(1e-3 * rng_))
+        cz.compress_field(f, eps, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")  # warm-up
+        ev[0].record(stream)
+        cf = cz.compress_field(f, eps, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
+        ev[1].record(stream)
+        data, off = cf.to_device()
+        ev[2].record(stream)
+        st = cz.diff_field(data, off, f.shape, f, WTYPE, SHUFFLE, encoder="lz4", file_bytes=cf.nbytes, out=dec)
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        c_ms, d_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
+        tot_c += c_ms
+        tot_d += d_ms
+        psnr = 20 * np.log10(rng_ / (2 * np.sqrt(st["e_2"] / st["n"])))
+        rf = cz.refit_field(f, eps, REFIT_ITERS, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
+        rd, ro = rf.to_device()
+        sr = cz.diff_field(rd, ro, f.shape, f, WTYPE, SHUFFLE, encoder="lz4", file_bytes=rf.nbytes, out=dec)
+        psnr_r = 20 * np.log10(rng_ / (2 * np.sqrt(sr["e_2"] / sr["n"])))
+        out["per_field"].append({"field": name, "compress_gbs": f.numel() * 4 / (c_ms * 1e-3) / 1e9,
+                                 "decompress_gbs": f.numel() * 4 / (d_ms * 1e-3) / 1e9,
+                                 "ratio": f.numel() * 4 / cf.nbytes, "psnr_db": psnr, "max_abs_err": st["e_inf"],
+                                 "res_line": st["res_line"],
+                                 "refit": {"ratio": f.numel() * 4 / rf.nbytes, "psnr_db": psnr_r,
+                                           "gain_db": psnr_r - psnr, "pre_lz4_bytes_equal": rf.raw_bytes == cf.raw_bytes}})
+        del data, off, rd, ro
+    out["compress_gbs"] = out["total_bytes"] / (tot_c * 1e-3) / 1e9
+    out["decompress_gbs"] = out["total_bytes"] / (tot_d * 1e-3) / 1e9
+    print(json.dumps({"stress": out}), flush=True)
+
+
 def run_reference(args, rank, world):
     """CPU implementation of the path on the host cores (rank 0 only)."""
     if rank != 0:
@@ -414,7 +465,11 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--stress", action="store_true", help="five 1024^3 fields, refit on and off (own JSON line)")
     args = ap.parse_args()
+    if args.stress:
+        run_stress(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -101,7 +101,7 @@ def batch_shapes(n=96, seed=0):
     return shapes, thr
 
 
-def generate_torch(shape, seed=0, blobs=20, interfaces=3, noise_rms=0.05, mean=1.0, device="cuda"):
+def generate_torch(shape, seed=0, blobs=20, interfaces=3, noise_rms=0.05, mean=1.0, velocity=False, device="cuda"):
     """The generator of `generate` evaluated with torch on `device` in
     float32: same parameter draws (numpy, seeded), noise phases from a
     seeded torch generator. Statistically the same fields, not the same
@@ -115,7 +115,7 @@ def generate_torch(shape, seed=0, blobs=20, interfaces=3, noise_rms=0.05, mean=1
         return torch.arange(a, b, device=device, dtype=torch.float32)
 
     for _ in range(blobs):
-        a = rng.uniform(0.5, 2.0)
+        a = rng.uniform(0.5, 2.0) * (rng.choice([-1.0, 1.0]) if velocity else 1.0)
         sig = rng.uniform(4.0, 16.0)
         cz, cy, cx = rng.uniform(0, nz), rng.uniform(0, ny), rng.uniform(0, nx)
         (z0, z1), (y0, y1), (x0, x1) = _box(cz, 8 * sig, nz), _box(cy, 8 * sig, ny), _box(cx, 8 * sig, nx)
@@ -143,5 +143,11 @@ def generate_torch(shape, seed=0, blobs=20, interfaces=3, noise_rms=0.05, mean=1
         r = torch.sqrt((ar(z0, z1)[:, None, None] - cz) ** 2 + (ar(y0, y1)[None, :, None] - cy) ** 2 +
                        (ar(x0, x1)[None, None, :] - cx) ** 2)
         f[z0:z1, y0:y1, x0:x1] += 0.5 * (1.0 - torch.tanh((r - r0) / 2.0))
-    f += mean - f.mean()
+    if velocity:
+        f -= f.mean()
+        s = f.std()
+        if s > 0:
+            f /= s
+    else:
+        f += mean - f.mean()
     return f.contiguous()
