@@ -63,7 +63,8 @@ def context(device=0):
 
 
 def params(eps, wtype=1, zerobits=0, shuffle=False, encoder="none", blocks_per_chunk=1):
-    enc = {"none": _lib.ENCODER_NONE, "lz4": _lib.ENCODER_LZ4}[encoder] if isinstance(encoder, str) else int(encoder)
+    enc = {"none": _lib.ENCODER_NONE, "lz4": _lib.ENCODER_LZ4, "zlib": _lib.ENCODER_ZLIB}[encoder] \
+        if isinstance(encoder, str) else int(encoder)
     return Params(float(eps), int(wtype), int(zerobits), 1 if shuffle else 0, enc, int(blocks_per_chunk))
 
 
@@ -129,6 +130,18 @@ def lz4_decompress(data, cap, device=0):
     dst = np.zeros(max(cap, 1), np.uint8)
     n = C.c_int(0)
     rc = ctx.L.cz_lz4_decompress(ctx.h, _u8(src) if src.size else None, src.size, _u8(dst), cap, C.byref(n))
+    ctx.check(rc)
+    return dst[: n.value].tobytes()
+
+
+def zlib_decompress(data, cap, device=0):
+    """zdecompress's zlib branch on the GPU; raises CzError on malformed
+    input (the Adler-32 trailer is checked)."""
+    ctx = context(device)
+    src = np.frombuffer(bytes(data), np.uint8).copy()
+    dst = np.zeros(max(cap, 1), np.uint8)
+    n = C.c_int(0)
+    rc = ctx.L.cz_zlib_decompress(ctx.h, _u8(src) if src.size else None, src.size, _u8(dst), cap, C.byref(n))
     ctx.check(rc)
     return dst[: n.value].tobytes()
 

@@ -118,8 +118,8 @@ int check_params(cz_ctx *c, const cz_params *p)
 {
     if (!p) return fail(c, CZ_E_ARG, "params is NULL");
     if (p->zerobits < 0 || p->zerobits > 31) return fail(c, CZ_E_ARG, "zerobits must be in [0,31]");
-    if (p->encoder != CZ_ENCODER_NONE && p->encoder != CZ_ENCODER_LZ4)
-        return fail(c, CZ_E_ARG, "encoder must be CZ_ENCODER_NONE or CZ_ENCODER_LZ4");
+    if (p->encoder != CZ_ENCODER_NONE && p->encoder != CZ_ENCODER_LZ4 && p->encoder != CZ_ENCODER_ZLIB)
+        return fail(c, CZ_E_ARG, "encoder must be CZ_ENCODER_NONE, CZ_ENCODER_LZ4 or CZ_ENCODER_ZLIB");
     if (p->blocks_per_chunk < 1 || p->blocks_per_chunk > 64) return fail(c, CZ_E_ARG, "blocks_per_chunk must be in [1,64]");
     if (!(p->eps == p->eps)) return fail(c, CZ_E_ARG, "eps is NaN");
     return CZ_OK;
@@ -177,6 +177,7 @@ struct Job {
 int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const cz_params *p, int refit_iters,
             cudaStream_t st, Job &job)
 {
+    if (p->encoder == CZ_ENCODER_ZLIB) return fail(c, CZ_E_ARG, "zlib encoding is decode-only here: use lz4 or none");
     const int bpc = p->blocks_per_chunk;
     const long long nch_ll = (nblocks + bpc - 1) / bpc;
     if (nch_ll > 0x7fffffffLL) return fail(c, CZ_E_ARG, "too many chunks");
@@ -320,7 +321,7 @@ int decompress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long n
     CZ_TRY(grow(c, c->status, sizeof(int) * nblocks));
     CZ_TRY(grow(c, c->queue, 64));
     CZ_TRY(grow(c, c->flag, 64));
-    if (encoder == CZ_ENCODER_LZ4) CZ_TRY(grow(c, c->dec, (size_t)nchunks * dcap));
+    if (encoder != CZ_ENCODER_NONE) CZ_TRY(grow(c, c->dec, (size_t)nchunks * dcap));
     // pinned scratch: [fields | flag (64 B) | block map]
     const size_t pin_fields = (sizeof(CzField) * fields.size() + 63) / 64 * 64;
     const size_t map_bytes = h_block_chunk ? sizeof(int) * 2 * nblocks : 0;
@@ -329,13 +330,19 @@ int decompress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long n
     CZ_CUDA(c, cudaMemcpyAsync(c->fields.p, c->pin, sizeof(CzField) * fields.size(), cudaMemcpyHostToDevice, st));
     CZ_CUDA(c, cudaMemsetAsync(c->queue.p, 0, 64, st));
     CZ_CUDA(c, cudaMemsetAsync(c->flag.p, 0, 64, st));
-    const int raw = encoder != CZ_ENCODER_LZ4;
+    const int raw = encoder == CZ_ENCODER_NONE;
     CZ_TRY(mark(c, 0, st));
     CZ_CUDA(c, cz_launch_decode_setup(nchunks, d_off, P<int>(c->in_len), P<long long>(c->dec_off), P<int>(c->dec_cap),
                                       dcap, raw, st));
     const uint8_t *base = d_data;
     const int *dlen = P<int>(c->in_len);
-    if (!raw) {
+    if (encoder == CZ_ENCODER_ZLIB) {
+        CZ_CUDA(c, cz_launch_inflate(d_data, d_off, P<int>(c->in_len), nchunks, P<uint8_t>(c->dec),
+                                     P<long long>(c->dec_off), P<int>(c->dec_cap), P<int>(c->dec_len),
+                                     std::min(nchunks, c->sms * 32), st));
+        base = P<uint8_t>(c->dec);
+        dlen = P<int>(c->dec_len);
+    } else if (!raw) {
         const int lzgrid = std::max(1, std::min((nchunks + 3) / 4, c->sms * 8));
         CZ_CUDA(c, cz_launch_lz4_decode(d_data, d_off, P<int>(c->in_len), nchunks, P<uint8_t>(c->dec),
                                         P<long long>(c->dec_off), P<int>(c->dec_cap), P<int>(c->dec_len), lzgrid, st));
@@ -871,6 +878,36 @@ int cz_lz4_decompress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, in
     return CZ_OK;
 }
 
+int cz_zlib_decompress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out)
+{
+    if (!c || (!src && isize) || !dst || !out || isize < 0 || cap < 0) return fail(c, CZ_E_ARG, "bad zlib arguments");
+    CZ_TRY(set_device(c));
+    const size_t in_bytes = ((size_t)isize + 64 + 15) / 16 * 16;
+    CZ_TRY(grow(c, c->tmp_in, in_bytes + 64 + (size_t)cap + 64));
+    CZ_TRY(grow_pin(c, 4096));
+    uint8_t *d = P<uint8_t>(c->tmp_in);
+    uint8_t *meta = d + in_bytes;
+    uint8_t *dout = meta + 64;
+    long long *h = reinterpret_cast<long long *>(c->pin);
+    h[0] = 0;
+    h[1] = 0;
+    reinterpret_cast<int *>(h + 2)[0] = isize;
+    reinterpret_cast<int *>(h + 2)[1] = cap;
+    if (isize) CZ_CUDA(c, cudaMemcpy(d, src, isize, cudaMemcpyHostToDevice));
+    CZ_CUDA(c, cudaMemcpy(meta, h, 24, cudaMemcpyHostToDevice));
+    long long *doff = reinterpret_cast<long long *>(meta);
+    int *dlen = reinterpret_cast<int *>(meta + 16);
+    int *dcap = reinterpret_cast<int *>(meta + 20);
+    int *dres = reinterpret_cast<int *>(meta + 24);
+    CZ_CUDA(c, cz_launch_inflate(d, doff, dlen, 1, dout, doff + 1, dcap, dres, 1, nullptr));
+    int n = 0;
+    CZ_CUDA(c, cudaMemcpy(&n, dres, 4, cudaMemcpyDeviceToHost));
+    *out = n;
+    if (n < 0) return fail(c, CZ_E_CORRUPT, "malformed zlib input");
+    if (n) CZ_CUDA(c, cudaMemcpy(dst, dout, n, cudaMemcpyDeviceToHost));
+    return CZ_OK;
+}
+
 // ---------------------------------------------------------------- .cz images
 long long cz_file_bytes(cz_ctx *c, const cz_stream *s, int nx, int ny, int nz, const cz_params *p)
 {
@@ -1163,7 +1200,7 @@ int cz_decompress_image(cz_ctx *c, const uint8_t *img, long long size, int wtype
     if (czf::parse_image(img, size, ps, err) != 0) return fail(c, CZ_E_CORRUPT, err);
     if (ps.wavelets != czf::wavelet_name(wtype))
         return fail(c, CZ_E_ARG, "file wavelets " + ps.wavelets + " do not match wtype " + std::to_string(wtype));
-    if (ps.encoder != CZ_ENCODER_NONE && ps.encoder != CZ_ENCODER_LZ4)
+    if (ps.encoder != CZ_ENCODER_NONE && ps.encoder != CZ_ENCODER_LZ4 && ps.encoder != CZ_ENCODER_ZLIB)
         return fail(c, CZ_E_ARG, "unsupported encoder in file");
     const int nx = ps.bx * 32, ny = ps.by * 32, nz = ps.bz * 32;
     const long long nelem = (long long)nx * ny * nz;

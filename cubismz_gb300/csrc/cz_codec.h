@@ -95,3 +95,7 @@ cudaError_t cz_launch_from_zfastest(const void *in, int bytes, int nch, int ch, 
                                     cudaStream_t st);
 cudaError_t cz_launch_to_zfastest(const float *in, int nx, int ny, int nz, int nch, int ch, float *out,
                                   cudaStream_t st);
+
+// zlib streams (cz_zlib.cu): one warp per chunk; out_len[c] = bytes or < 0.
+cudaError_t cz_launch_inflate(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks, uint8_t *out,
+                              const long long *out_off, const int *out_cap, int *out_len, int grid, cudaStream_t st);

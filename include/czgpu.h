@@ -43,6 +43,7 @@ extern "C" {
 
 #define CZ_ENCODER_NONE 0 /* "Encoder: none"  (CompressionEncoders.h:240-246) */
 #define CZ_ENCODER_LZ4 1  /* "Encoder: lz4"   (CompressionEncoders.h:192-238) */
+#define CZ_ENCODER_ZLIB 2 /* "Encoder: zlib"  (CompressionEncoders.h:116-190); decode only */
 
 typedef struct cz_ctx cz_ctx;
 
@@ -52,7 +53,8 @@ typedef struct cz_ctx cz_ctx;
  *              (any other value behaves as 3, WaveletsOnInterval.h:154)
  *   zerobits   0 or n: clear the n low bits of every survivor (-D_ZEROBITS_=n)
  *   shuffle    0/1: byte-plane shuffle of the survivors (-D_USE_SHUFFLE3_)
- *   encoder    CZ_ENCODER_NONE or CZ_ENCODER_LZ4
+ *   encoder    CZ_ENCODER_NONE, CZ_ENCODER_LZ4, or CZ_ENCODER_ZLIB (reading
+ *              reference zlib streams and files; not for compression)
  *   blocks_per_chunk  records per lossless chunk (1 is the default) */
 typedef struct {
     float eps;
@@ -115,6 +117,11 @@ int cz_lz4_compress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, in
 /* Decode with the acceptance rules of LZ4_uncompress_unknownOutputSize
  * (lz4.c:802-905); *out = decoded size. Malformed input -> CZ_E_CORRUPT. */
 int cz_lz4_decompress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out);
+/* zdecompress's zlib branch (CompressionEncoders.h:48-88: inflateInit +
+ * inflate(Z_FINISH)): a zlib stream (RFC 1950/1951) decoded on the GPU.
+ * The Adler-32 trailer is checked; malformed or truncated input returns
+ * CZ_E_CORRUPT (the reference accepts any non-zero inflate return). */
+int cz_zlib_decompress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out);
 
 /* ---- field level (device buffers) ------------------------------------- */
 /* Compress a field d_field[nz][ny][nx] (extents multiples of 32) into the

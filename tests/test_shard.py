@@ -100,3 +100,22 @@ def test_single_rank_file_is_the_reference_writers(lib, small_field):
         shard.write_file(mine, part, n, small_field.shape, api.params(eps, 1, 4, True, "none", 15))
         O.ref_write_cz(L, small_field, eps, 1, theirs, 1, 1)
         assert open(mine, "rb").read() == open(theirs, "rb").read()
+
+
+def test_single_rank_zlib_file_is_the_reference_writers(lib, demo_field):
+    """Encoder zlib, 15 records per chunk, one thread: the file assembled
+    from zlib chunks equals the reference writer's byte for byte."""
+    L = O.ref(0, 0, "zlib")
+    if L is None:
+        pytest.skip("reference build not available")
+    from cubismz_gb300 import api, shard
+    from tests.helpers import zlib_chunks
+    raw, off = O.field_compress(demo_field, 5e-5, 3, 0, 0, 0, 1)
+    z = zlib_chunks(raw, off, 15, 64)
+    offs = np.concatenate([[0], np.cumsum([len(c) for c in z])]).astype(np.int64)
+    part, n = shard.part_from_host(np.frombuffer(b"".join(z), np.uint8), offs)
+    with tempfile.TemporaryDirectory() as d:
+        mine, theirs = os.path.join(d, "a.cz"), os.path.join(d, "b.cz")
+        shard.write_file(mine, part, n, demo_field.shape, api.params(5e-5, 3, 0, False, "zlib", 15))
+        O.ref_write_cz(L, demo_field, 5e-5, 3, theirs, 1, 1)
+        assert open(mine, "rb").read() == open(theirs, "rb").read()
