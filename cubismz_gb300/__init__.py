@@ -8,10 +8,10 @@ from .api import (Context, CompressedField, WaveletCompressor, compress_field, c
                   decompress_field, decompress_image, diff_field, field_from_zfastest,
                   field_to_zfastest, image_info, iwt_adjoint, iwt_linear, lz4_compress,
                   lz4_decompress, params, Plan, refit_field, res_line,
-                  zlib_decompress)
+                  zlib_compress, zlib_decompress)
 from ._lib import CzError
 
 __all__ = ["Context", "CompressedField", "WaveletCompressor", "compress_field", "compress_to_image", "context",
            "decompress_field", "decompress_image", "diff_field", "field_from_zfastest",
            "field_to_zfastest", "image_info", "iwt_adjoint", "iwt_linear", "lz4_compress",
-           "lz4_decompress", "params", "Plan", "refit_field", "res_line", "zlib_decompress", "CzError"]
+           "lz4_decompress", "params", "Plan", "refit_field", "res_line", "zlib_compress", "zlib_decompress", "CzError"]

@@ -35,7 +35,7 @@ EXPORTS = [
     "cz_mini_bytes", "cz_mini_write", "cz_part_bytes", "cz_part_write", "cz_stream_part", "cz_tail_bytes",
     "cz_tail_write", "cz_plan_create", "cz_plan_launch", "cz_plan_result", "cz_plan_info", "cz_plan_last_error",
     "cz_plan_destroy", "cz_field_diff", "cz_res_line", "cz_field_from_zfastest", "cz_field_to_zfastest",
-    "cz_zlib_decompress",
+    "cz_zlib_decompress", "cz_zlib_bound", "cz_zlib_compress",
 ]
 NOALLOC_MAX_BLOCKS = 16
 
@@ -81,6 +81,8 @@ def load():
     L.cz_lz4_compress.argtypes = [vp, u8p, C.c_int, u8p, C.c_int, ip]
     L.cz_lz4_decompress.argtypes = [vp, u8p, C.c_int, u8p, C.c_int, ip]
     L.cz_zlib_decompress.argtypes = [vp, u8p, C.c_int, u8p, C.c_int, ip]
+    L.cz_zlib_bound.argtypes = [C.c_int]
+    L.cz_zlib_compress.argtypes = [vp, u8p, C.c_int, u8p, C.c_int, ip]
     L.cz_field_compress.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.POINTER(Params), vp, C.POINTER(Stream)]
     L.cz_stream_copy.argtypes = [vp, C.POINTER(Stream), vp, vp, vp]
     L.cz_field_decompress.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(Params), vp, vp]

@@ -134,6 +134,18 @@ def lz4_decompress(data, cap, device=0):
     return dst[: n.value].tobytes()
 
 
+def zlib_compress(data, device=0):
+    """deflate_inplace's zlib branch on the GPU (host bytes in, a zlib
+    stream out; any inflate reads it)."""
+    ctx = context(device)
+    src = np.frombuffer(bytes(data), np.uint8).copy()
+    cap = ctx.L.cz_zlib_bound(src.size)
+    dst = np.zeros(max(cap, 1), np.uint8)
+    n = C.c_int(0)
+    ctx.check(ctx.L.cz_zlib_compress(ctx.h, _u8(src) if src.size else None, src.size, _u8(dst), cap, C.byref(n)))
+    return dst[: n.value].tobytes()
+
+
 def zlib_decompress(data, cap, device=0):
     """zdecompress's zlib branch on the GPU; raises CzError on malformed
     input (the Adler-32 trailer is checked)."""

@@ -32,6 +32,12 @@ struct DevBuf {
 };
 
 constexpr long long lz4_bound_ll(long long n) { return n + n / 255 + 16; }
+// zlib stream bound: header, Adler-32, and per block (every block but the
+// last covers at least 1024 bytes; none is larger than its stored coding)
+// at most 6 bytes beyond its data
+constexpr long long zlib_bound_ll(long long n) { return n + 6 * (n / 1024 + 2) + 8; }
+// DEFLATE parse records of a chunk (cz_launch_lz77_parse)
+constexpr long long seq_bound_ll(long long n) { return 8 * (n / 4 + 2); }
 
 }  // namespace
 
@@ -41,7 +47,7 @@ struct cz_ctx {
     std::string err;
     DevBuf fields, stage, rec_bytes, chunk_in, in_off, in_len, blk_dst, lz_off, lz_out, lz_len, out_off, out_data,
         queue, status, flag, rec_off, dec, dec_off, dec_cap, dec_len, raw_off, chunk_rec, block_chunk, block_subid,
-        tmp_field, tmp_in, refit, diff;
+        tmp_field, tmp_in, refit, diff, zout, zoff, zlen;
     void *pin = nullptr;  // small pinned host scratch
     size_t pin_cap = 0;
     // geometry of the last compressed stream
@@ -170,14 +176,13 @@ void collect(cz_ctx *c)
 struct Job {
     long long nblocks = 0;
     int nfields = 0, nchunks = 0, bpc = 1, lz_warps = 4, refit_iters = 0;
-    long long lz_slot = 0;
+    long long lz_slot = 0, z_slot = 0;  // per chunk: LZ4 output or DEFLATE parse; zlib output
     cz_params p{};
 };
 
 int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, const cz_params *p, int refit_iters,
             cudaStream_t st, Job &job)
 {
-    if (p->encoder == CZ_ENCODER_ZLIB) return fail(c, CZ_E_ARG, "zlib encoding is decode-only here: use lz4 or none");
     const int bpc = p->blocks_per_chunk;
     const long long nch_ll = (nblocks + bpc - 1) / bpc;
     if (nch_ll > 0x7fffffffLL) return fail(c, CZ_E_ARG, "too many chunks");
@@ -187,7 +192,10 @@ int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, co
     job.bpc = bpc;
     job.p = *p;
     job.refit_iters = refit_iters;
-    job.lz_slot = (lz4_bound_ll((long long)bpc * kSlotBytes) + 15) / 16 * 16;
+    const long long chunk_max = (long long)bpc * kSlotBytes;
+    const bool zlib = p->encoder == CZ_ENCODER_ZLIB;
+    job.lz_slot = ((zlib ? seq_bound_ll(chunk_max) : lz4_bound_ll(chunk_max)) + 15) / 16 * 16;
+    job.z_slot = zlib ? (zlib_bound_ll(chunk_max) + 16 + 15) / 16 * 16 : 0;
     const int nchunks = job.nchunks;
     CZ_TRY(grow(c, c->fields, sizeof(CzField) * fields.size()));
     CZ_TRY(grow(c, c->stage, (size_t)nblocks * kSlotBytes));
@@ -204,10 +212,15 @@ int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, co
         CZ_TRY(grow(c, c->blk_dst, sizeof(long long) * nblocks));
         CZ_TRY(grow(c, c->chunk_in, (size_t)nchunks * bpc * kSlotBytes));
     }
-    if (p->encoder == CZ_ENCODER_LZ4) CZ_TRY(grow(c, c->lz_out, (size_t)nchunks * job.lz_slot));
+    if (p->encoder != CZ_ENCODER_NONE) CZ_TRY(grow(c, c->lz_out, (size_t)nchunks * job.lz_slot));
+    if (zlib) {
+        CZ_TRY(grow(c, c->zout, (size_t)nchunks * job.z_slot));
+        CZ_TRY(grow(c, c->zoff, sizeof(long long) * nchunks));
+        CZ_TRY(grow(c, c->zlen, sizeof(int) * nchunks));
+    }
     // the gathered stream is bounded by the lossless bound of every chunk
-    const size_t out_cap =
-        (size_t)nchunks * (p->encoder == CZ_ENCODER_LZ4 ? job.lz_slot : (long long)bpc * kSlotBytes);
+    const size_t out_cap = (size_t)nchunks * (p->encoder == CZ_ENCODER_LZ4 ? job.lz_slot
+                                                                           : (zlib ? job.z_slot : chunk_max));
     CZ_TRY(grow(c, c->out_data, out_cap));
     const int grid = (int)std::min<long long>(nblocks, c->sms);
     if (refit_iters > 0) CZ_TRY(grow(c, c->refit, sizeof(float) * cz_refit_scratch_floats(grid)));
@@ -259,6 +272,20 @@ int enqueue(cz_ctx *c, const Job &job, cudaStream_t st, bool marks)
         gsrc = P<uint8_t>(c->lz_out);
         gsrc_off = P<long long>(c->lz_off);
         glen = P<int>(c->lz_len);
+    } else if (p->encoder == CZ_ENCODER_ZLIB) {
+        const int pgrid = std::max(1, std::min((nchunks + 3) / 4, c->sms * 8));
+        CZ_CUDA(c, cz_launch_lz77_parse(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
+                                        P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<int>(c->lz_len),
+                                        p->shuffle ? 1 : 0, pgrid, st));
+        CZ_CUDA(c, cz_launch_deflate(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), P<uint8_t>(c->lz_out),
+                                     P<long long>(c->lz_off), P<int>(c->lz_len), nchunks, p->shuffle ? 1 : 0,
+                                     P<uint8_t>(c->zout),
+                                     job.z_slot, P<long long>(c->zoff), P<int>(c->zlen),
+                                     std::max(1, std::min((nchunks + 3) / 4, c->sms * 5)), st));
+        CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->zlen), nchunks, P<int>(c->flag), st));
+        gsrc = P<uint8_t>(c->zout);
+        gsrc_off = P<long long>(c->zoff);
+        glen = P<int>(c->zlen);
     }
     if (marks) CZ_TRY(mark(c, 2, st));
     CZ_CUDA(c, cz_launch_scan(glen, nchunks, P<long long>(c->out_off), st));
@@ -275,7 +302,8 @@ int finish(cz_ctx *c, const Job &job, cudaStream_t st, cz_stream *out)
     CZ_CUDA(c, cudaMemcpyAsync(&h[1], P<long long>(c->raw_off) + nchunks, 8, cudaMemcpyDeviceToHost, st));
     CZ_CUDA(c, cudaMemcpyAsync(&h[2], c->flag.p, 4, cudaMemcpyDeviceToHost, st));
     CZ_CUDA(c, cudaStreamSynchronize(st));
-    if (reinterpret_cast<int *>(&h[2])[0] != 0) return fail(c, CZ_E_CUDA, "LZ4 encoder output exceeded its bound");
+    if (reinterpret_cast<int *>(&h[2])[0] != 0)
+        return fail(c, CZ_E_CUDA, "lossless encoder output exceeded its bound");
     c->nblocks = job.nblocks;
     c->nchunks = nchunks;
     c->bpc = job.bpc;
@@ -415,7 +443,7 @@ int cz_destroy(cz_ctx *c)
 {
     if (!c) return CZ_OK;
     cudaSetDevice(c->device);
-    DevBuf *all[] = {&c->diff, &c->refit, &c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
+    DevBuf *all[] = {&c->zout, &c->zoff, &c->zlen, &c->diff, &c->refit, &c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
                      &c->blk_dst, &c->lz_off,  &c->lz_out,    &c->lz_len,    &c->out_off,     &c->out_data,
                      &c->queue,   &c->status,  &c->flag,      &c->rec_off,   &c->dec,         &c->dec_off,
                      &c->dec_cap, &c->dec_len, &c->raw_off,   &c->chunk_rec, &c->block_chunk, &c->block_subid,
@@ -848,6 +876,42 @@ int cz_lz4_compress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int 
     return CZ_OK;
 }
 
+int cz_zlib_bound(int isize) { return isize < 0 ? 0 : (int)zlib_bound_ll(isize); }
+
+int cz_zlib_compress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out)
+{
+    if (!c || (!src && isize) || !dst || !out || isize < 0 || isize > (1 << 24) - 64)
+        return fail(c, CZ_E_ARG, "bad zlib arguments");
+    CZ_TRY(set_device(c));
+    const size_t in_bytes = ((size_t)isize + 64 + 15) / 16 * 16;
+    const size_t seq_bytes = ((size_t)seq_bound_ll(isize) + 15) / 16 * 16;
+    const size_t zbytes = ((size_t)zlib_bound_ll(isize) + 16 + 15) / 16 * 16;
+    CZ_TRY(grow(c, c->tmp_in, in_bytes + 64 + seq_bytes + zbytes));
+    CZ_TRY(grow_pin(c, 4096));
+    uint8_t *d = P<uint8_t>(c->tmp_in);
+    uint8_t *meta = d + in_bytes;  // in_off, seq_off, zoff (8 each), in_len, seq_len, zlen (4 each)
+    uint8_t *dseq = meta + 64, *dz = dseq + seq_bytes;
+    long long *h = reinterpret_cast<long long *>(c->pin);
+    h[0] = 0;
+    h[1] = 0;
+    h[2] = 0;
+    reinterpret_cast<int *>(h + 3)[0] = isize;
+    if (isize) CZ_CUDA(c, cudaMemcpy(d, src, isize, cudaMemcpyHostToDevice));
+    CZ_CUDA(c, cudaMemcpy(meta, h, 32, cudaMemcpyHostToDevice));
+    long long *doff = reinterpret_cast<long long *>(meta);
+    int *dlen = reinterpret_cast<int *>(meta + 24);
+    CZ_CUDA(c, cz_launch_lz77_parse(d, doff, dlen, 1, dseq, doff + 1, dlen + 1, 0, 1, nullptr));
+    CZ_CUDA(c, cz_launch_deflate(d, doff, dlen, dseq, doff + 1, dlen + 1, 1, 0, dz, (long long)zbytes, doff + 2,
+                                 dlen + 2, 1, nullptr));
+    int n = 0;
+    CZ_CUDA(c, cudaMemcpy(&n, dlen + 2, 4, cudaMemcpyDeviceToHost));
+    if (n < 0) return fail(c, CZ_E_CUDA, "zlib encoder failed");
+    if (n > cap) return fail(c, CZ_E_SPACE, "zlib output buffer too small");
+    CZ_CUDA(c, cudaMemcpy(dst, dz, n, cudaMemcpyDeviceToHost));
+    *out = n;
+    return CZ_OK;
+}
+
 int cz_lz4_decompress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out)
 {
     if (!c || (!src && isize) || !dst || !out || isize < 0 || cap < 0) return fail(c, CZ_E_ARG, "bad LZ4 arguments");
@@ -1006,7 +1070,7 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
     cudaStream_t st = (cudaStream_t)stream;
     const size_t bytes = sizeof(float) * (size_t)nx * ny * nz;
     CZ_TRY(grow(c, c->tmp_field, bytes));
-    if (p->blocks_per_chunk != 1) {  // chunks of several records: whole-field path
+    if (p->blocks_per_chunk != 1 || p->encoder == CZ_ENCODER_ZLIB) {  // whole-field path
         CZ_CUDA(c, cudaMemcpyAsync(c->tmp_field.p, h_field, bytes, cudaMemcpyHostToDevice, st));
         cz_stream s;
         CZ_TRY(cz_field_compress(c, P<float>(c->tmp_field), nx, ny, nz, p, stream, &s));

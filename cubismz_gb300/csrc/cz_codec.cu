@@ -327,16 +327,42 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
 }
 
 // Totals over blocks, in block order: {e_inf, n_inf, e_1, e_2, n_1, n_2, min, max}.
-__global__ void diff_total_kernel(const double *per_block, long long nblocks, double *total)
+// Field totals of the per-block statistics, in a fixed order: thread group j
+// (of kDiffGroups) folds blocks j, j + kDiffGroups, ... in turn (four loads
+// in flight, folded in block order), then the groups fold in order j = 0, 1,
+// ... Deterministic for a given block count.
+constexpr int kDiffGroups = 128;
+__device__ __forceinline__ double diff_fold(int k, double r, double x)
 {
-    const int k = threadIdx.x;
-    if (k >= 8) return;
-    double r = per_block[k];
-    for (long long g = 1; g < nblocks; ++g) {
-        const double x = per_block[g * 8 + k];
-        r = (k == 0 || k == 1 || k == 7) ? fmax(r, x) : (k == 6 ? fmin(r, x) : r + x);
+    return (k == 0 || k == 1 || k == 7) ? fmax(r, x) : (k == 6 ? fmin(r, x) : r + x);
+}
+__global__ void __launch_bounds__(8 * kDiffGroups)
+diff_total_kernel(const double *per_block, long long nblocks, double *total)
+{
+    __shared__ double part[kDiffGroups][8];
+    __shared__ int have[kDiffGroups];
+    const int k = threadIdx.x & 7, j = threadIdx.x >> 3;
+    double r = 0.0;
+    long long g = j;
+    if (g < nblocks) {
+        r = per_block[g * 8 + k];
+        g += kDiffGroups;
     }
-    total[k] = r;
+    for (; g + 3 * kDiffGroups < nblocks; g += 4 * kDiffGroups) {
+        const double x0 = per_block[g * 8 + k], x1 = per_block[(g + kDiffGroups) * 8 + k];
+        const double x2 = per_block[(g + 2 * kDiffGroups) * 8 + k], x3 = per_block[(g + 3 * kDiffGroups) * 8 + k];
+        r = diff_fold(k, diff_fold(k, diff_fold(k, diff_fold(k, r, x0), x1), x2), x3);
+    }
+    for (; g < nblocks; g += kDiffGroups) r = diff_fold(k, r, per_block[g * 8 + k]);
+    part[j][k] = r;
+    if (k == 0) have[j] = j < nblocks;
+    __syncthreads();
+    if (j == 0) {
+        double t = part[0][k];
+        for (int i = 1; i < kDiffGroups; ++i)
+            if (have[i]) t = diff_fold(k, t, part[i][k]);
+        total[k] = t;
+    }
 }
 
 }  // namespace cz
@@ -407,6 +433,7 @@ cudaError_t cz_launch_decode(int wtype, const CzField *fields, int nfields, long
 
 cudaError_t cz_launch_diff_total(const double *per_block, long long nblocks, double *total, cudaStream_t st)
 {
-    diff_total_kernel<<<1, 32, 0, st>>>(per_block, nblocks, total);
+    if (nblocks < 1) return cudaErrorInvalidValue;
+    diff_total_kernel<<<1, 8 * kDiffGroups, 0, st>>>(per_block, nblocks, total);
     return cudaGetLastError();
 }

@@ -51,6 +51,21 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
                                  int grid, cudaStream_t st);
+// The LZ77 parse of the LZ4 encoder for DEFLATE: distances up to 32 KiB,
+// 8-byte sequence records (zl::seq_pack) per chunk at seq + seq_off[c]
+// (capacity 8 * (in_len/4 + 2) bytes); seq_bytes[c] = record bytes.
+cudaError_t cz_launch_lz77_parse(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
+                                 uint8_t *seq, const long long *seq_off, int *seq_bytes, int records, int grid,
+                                 cudaStream_t st);
+// zlib streams (RFC 1950/1951) from the parse: chunk c at out + c * out_slot
+// (out_slot >= cz_zlib_bound of the chunk), out_off[c] = c * out_slot,
+// out_len[c] = stream bytes, -1 for a bad parse, -2..-4 for an internal
+// inconsistency (never written past the slot).
+// records: chunks of shuffled block records (blocks end at mask and planes).
+cudaError_t cz_launch_deflate(const uint8_t *in, const long long *in_off, const int *in_len, const uint8_t *seq,
+                              const long long *seq_off, const int *seq_bytes, int nchunks, int records,
+                              uint8_t *out, long long out_slot, long long *out_off, int *out_len, int grid,
+                              cudaStream_t st);
 cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, const int *out_cap, int *out_len, int grid,
                                  cudaStream_t st);

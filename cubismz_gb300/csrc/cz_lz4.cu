@@ -31,6 +31,7 @@
 // replayed in order, each by the whole warp (overlapping matches repeat
 // their first `offset` bytes, the byte-serial copy semantics).
 #include "cz_codec.h"
+#include "cz_deflate.cuh"
 
 namespace cz {
 
@@ -161,11 +162,16 @@ __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, in
     return len < matchlimit - p ? len : matchlimit - p;
 }
 
-template <int kLzWarps>
+// SEQ: the parse for the DEFLATE encoder instead of LZ4 bytes -- distances up
+// to 32 KiB, and per kept sequence one 8-byte record (literal run, match
+// length, distance; zl::seq_pack) at out + out_off[c]; the last record holds
+// the tail literals. out_len[c] = record bytes, -1 past the capacity.
+template <int kLzWarps, bool SEQ>
 __global__ void __launch_bounds__(kLzWarps * 32)
 lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
                   uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records)
 {
+    constexpr int kMaxOff = SEQ ? zl::kMaxDist : 65535;
     __shared__ uint32_t table_all[kLzWarps][1 << kHashLog];
     __shared__ uint16_t info_all[kLzWarps][kSW];                // candidate offset per position, 0: none
     __shared__ uint32_t seq_all[kLzWarps][32][kMaxSeqLane];     // start - base | offset << 16
@@ -185,7 +191,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
         const uint8_t *src = in + in_off[c];
         const int L = in_len[c];
         uint8_t *dst = out + out_off[c];
-        const int cap = L + L / 255 + 16;
+        const int cap = SEQ ? 8 * (L / 4 + 2) : L + L / 255 + 16;
         for (int i = lane; i < (1 << kHashLog); i += 32) table[i] = kEmpty;
         __syncwarp();
         int pos = 0, anchor = 0, op = 0, miss = 0;
@@ -253,7 +259,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     const int p = wpos + j;
                     const int off = (int)(((uint32_t)p - (e[j] >> 14)) & kPosMask);
                     int v = 0;
-                    if (valid[j] && e[j] != kEmpty && (e[j] & 0x3fff) == tag[j] && off >= 1 && off <= 65535 && off <= p)
+                    if (valid[j] && e[j] != kEmpty && (e[j] & 0x3fff) == tag[j] && off >= 1 && off <= kMaxOff && off <= p)
                         v = off;  // the walk verifies and measures chosen candidates
                     if (valid[j]) info[p - base] = (uint16_t)v;
                     any_match |= v != 0;
@@ -317,7 +323,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 const int st = base + (int)(myseq[i] & 0xffff);
                 if (st < lit_from) continue;
                 const int l = st - lit_from, ml = mylen[i] - kMinMatch;
-                bytes += 1 + (l >= 15 ? len_bytes(l - 15) : 0) + l + 2 + (ml >= 15 ? len_bytes(ml - 15) : 0);
+                bytes += SEQ ? 8 : 1 + (l >= 15 ? len_bytes(l - 15) : 0) + l + 2 + (ml >= 15 ? len_bytes(ml - 15) : 0);
                 lit_from = st + mylen[i];
                 ++nkeep;
             }
@@ -334,7 +340,18 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             }
             if (lane == 0) nlong = 0;
             __syncwarp();
-            {
+            if (SEQ) {
+                int at = op + incl - bytes;
+                lit_from = myP;
+                for (int i = 0; i < ns; ++i) {
+                    const int st = base + (int)(myseq[i] & 0xffff);
+                    if (st < lit_from) continue;
+                    *reinterpret_cast<unsigned long long *>(dst + at) =
+                        zl::seq_pack(st - lit_from, mylen[i], (int)(myseq[i] >> 16));
+                    at += 8;
+                    lit_from = st + mylen[i];
+                }
+            } else {
                 int at = op + incl - bytes;
                 lit_from = myP;
                 for (int i = 0; i < ns; ++i) {
@@ -376,7 +393,14 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             anchor = P;
             pos = end > P ? end : P;
         }
-        if (!overflow) {
+        if (!overflow && SEQ) {
+            if (op + 8 > cap) {
+                overflow = true;
+            } else {
+                if (lane == 0) *reinterpret_cast<unsigned long long *>(dst + op) = zl::seq_pack(L - anchor, 0, 0);
+                op += 8;
+            }
+        } else if (!overflow) {
             const int lit = L - anchor;
             const int need = 1 + (lit >= 15 ? len_bytes(lit - 15) : 0) + lit;
             if (op + need > cap) {
@@ -807,10 +831,19 @@ cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, con
 {
     if (nchunks <= 0) return cudaSuccess;
     switch (warps) {
-    case 2: lz4_encode_kernel<2><<<grid, 64, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records); break;
-    case 8: lz4_encode_kernel<8><<<grid, 256, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records); break;
-    default: lz4_encode_kernel<4><<<grid, 128, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records);
+    case 2: lz4_encode_kernel<2, false><<<grid, 64, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records); break;
+    case 8: lz4_encode_kernel<8, false><<<grid, 256, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records); break;
+    default: lz4_encode_kernel<4, false><<<grid, 128, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t cz_launch_lz77_parse(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
+                                 uint8_t *seq, const long long *seq_off, int *seq_bytes, int records, int grid,
+                                 cudaStream_t st)
+{
+    if (nchunks <= 0) return cudaSuccess;
+    lz4_encode_kernel<4, true><<<grid, 128, 0, st>>>(in, in_off, in_len, nchunks, seq, seq_off, seq_bytes, records);
     return cudaGetLastError();
 }
 

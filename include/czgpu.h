@@ -43,7 +43,7 @@ extern "C" {
 
 #define CZ_ENCODER_NONE 0 /* "Encoder: none"  (CompressionEncoders.h:240-246) */
 #define CZ_ENCODER_LZ4 1  /* "Encoder: lz4"   (CompressionEncoders.h:192-238) */
-#define CZ_ENCODER_ZLIB 2 /* "Encoder: zlib"  (CompressionEncoders.h:116-190); decode only */
+#define CZ_ENCODER_ZLIB 2 /* "Encoder: zlib"  (CompressionEncoders.h:116-190) */
 
 typedef struct cz_ctx cz_ctx;
 
@@ -53,8 +53,7 @@ typedef struct cz_ctx cz_ctx;
  *              (any other value behaves as 3, WaveletsOnInterval.h:154)
  *   zerobits   0 or n: clear the n low bits of every survivor (-D_ZEROBITS_=n)
  *   shuffle    0/1: byte-plane shuffle of the survivors (-D_USE_SHUFFLE3_)
- *   encoder    CZ_ENCODER_NONE, CZ_ENCODER_LZ4, or CZ_ENCODER_ZLIB (reading
- *              reference zlib streams and files; not for compression)
+ *   encoder    CZ_ENCODER_NONE, CZ_ENCODER_LZ4, or CZ_ENCODER_ZLIB
  *   blocks_per_chunk  records per lossless chunk (1 is the default) */
 typedef struct {
     float eps;
@@ -117,6 +116,18 @@ int cz_lz4_compress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, in
 /* Decode with the acceptance rules of LZ4_uncompress_unknownOutputSize
  * (lz4.c:802-905); *out = decoded size. Malformed input -> CZ_E_CORRUPT. */
 int cz_lz4_decompress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out);
+/* Worst-case zlib stream size of cz_zlib_compress: isize + 6 * (isize/1024
+ * + 2) + 8 (no block is larger than its stored coding; blocks but the last
+ * cover at least 1 KiB). */
+int cz_zlib_bound(int isize);
+/* deflate_inplace's zlib branch (CompressionEncoders.h:116-190, a
+ * deflateInit(Z_DEFAULT_COMPRESSION) stream, SerializerIO_WaveletCompression_MPI_Simple.h:122)
+ * on the GPU: one zlib stream (RFC 1950) of DEFLATE blocks (RFC 1951) of
+ * up to 64 KiB each, every one dynamic Huffman, fixed Huffman or stored,
+ * whichever is smallest, from an LZ77 parse with a 32 KiB window. Any zlib
+ * inflate reads it; the bytes are not zlib's. isize < 2^24 - 64; cap >=
+ * cz_zlib_bound(isize) always suffices. */
+int cz_zlib_compress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out);
 /* zdecompress's zlib branch (CompressionEncoders.h:48-88: inflateInit +
  * inflate(Z_FINISH)): a zlib stream (RFC 1950/1951) decoded on the GPU.
  * The Adler-32 trailer is checked; malformed or truncated input returns

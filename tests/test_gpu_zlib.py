@@ -1,7 +1,9 @@
 """zlib streams on the GPU: every DEFLATE block type decodes like zlib
 itself, malformed input is rejected, and the published golden file (demo.h5,
 wtype 3, threshold 5e-5, Encoder: zlib, 15 records per chunk) decodes on the
-GPU to the published RES line."""
+GPU to the published RES line. Streams written by the GPU encoder decode
+with zlib to their input; fields and .cz files written with Encoder: zlib
+hold the oracle's records and decode bit-exactly."""
 import os
 import tempfile
 import zlib
@@ -76,3 +78,84 @@ def test_published_golden_zlib_file_on_gpu(cz, golden, demo_field):
     dec = cz.decompress_image(img, 3, False)
     assert np.array_equal(dec, O.field_decompress(raw, off, demo_field.shape, 3))
     assert cz.res_line(stats_f64(demo_field, dec), size) == golden["published_res"]
+
+
+def _encode_samples(small_field):
+    rng = np.random.default_rng(11)
+    unit = rng.integers(0, 256, 32768, np.uint8).tobytes()
+    return _samples(small_field) + [
+        b"ab", bytes(259), bytes(260), bytes(261), bytes(517), bytes(300000),
+        rng.integers(0, 256, 300000, np.uint8).tobytes(), unit + unit[:5000] + unit[:300],
+        bytes(rng.integers(0, 3, 100000, np.uint8)) * 2, (b"\x00" * 1000 + b"\x01" * 7) * 300]
+
+
+def test_deflate_streams_decode_with_zlib(cz, small_field):
+    """cz.zlib_compress: zlib and the GPU inflate read every stream back;
+    sizes stay within the stored bound."""
+    for d in _encode_samples(small_field):
+        z = cz.zlib_compress(d)
+        assert z[:2] == b"\x78\x9c"
+        assert zlib.decompress(z) == d, len(d)
+        assert cz.zlib_decompress(z, len(d)) == d
+        assert len(z) <= len(d) + 6 * (len(d) // 1024 + 2) + 8
+
+
+def test_deflate_ratio_against_zlib_default(cz, small_field):
+    """Field chunks of shuffled records (a DEFLATE block per mask and byte
+    plane) come out no larger than zlib at the reference's
+    Z_DEFAULT_COMPRESSION on the same records (2 % slack for the parse);
+    generic input within 15 %."""
+    import torch
+    f = torch.from_numpy(small_field).cuda()
+    eps = float(np.float32(1e-3 * (small_field.max() - small_field.min())))
+    raw, roff = O.field_compress(small_field, eps, 1, 4, 1, 0, 1)
+    cf = cz.compress_field(f, eps, 1, 4, True, encoder="zlib")
+    ref = sum(len(zlib.compress(bytes(raw[roff[i]:roff[i + 1]]), 6)) for i in range(len(roff) - 1))
+    assert cf.nbytes <= 1.02 * ref, (cf.nbytes, ref)
+    gpu = sum(len(cz.zlib_compress(bytes(raw[roff[i]:roff[i + 1]]))) for i in range(0, len(roff) - 1, 9))
+    ref = sum(len(zlib.compress(bytes(raw[roff[i]:roff[i + 1]]), 6)) for i in range(0, len(roff) - 1, 9))
+    assert gpu <= 1.15 * ref, (gpu, ref)
+
+
+@pytest.mark.parametrize("bpc", [1, 15])
+def test_field_with_zlib_encoder(cz, small_field, bpc):
+    """compress_field(encoder="zlib"): every chunk inflates (with zlib) to
+    the oracle's records, and the field decodes bit-exactly on the GPU."""
+    import torch
+    f = torch.from_numpy(small_field).cuda()
+    eps = float(np.float32(1e-3 * (small_field.max() - small_field.min())))
+    raw, roff = O.field_compress(small_field, eps, 1, 4, 1, 0, 1)
+    cf = cz.compress_field(f, eps, 1, 4, True, encoder="zlib", blocks_per_chunk=bpc)
+    data, off = cf.to_device()
+    h, o = data.cpu().numpy().tobytes(), off.cpu().numpy()
+    nb = len(roff) - 1
+    for c in range(len(o) - 1):
+        b0, b1 = c * bpc, min(nb, (c + 1) * bpc)
+        want = bytes(raw[roff[b0]:roff[b1]])
+        assert zlib.decompress(h[o[c]:o[c + 1]]) == want, c
+    dec = cz.decompress_field(data, off, small_field.shape, 1, True, encoder="zlib", blocks_per_chunk=bpc)
+    assert np.array_equal(dec.cpu().numpy(), O.field_decompress(raw, roff, small_field.shape, 1, 1))
+
+
+def test_zlib_cz_image(cz, small_field):
+    """A .cz image with Encoder: zlib from the GPU: header names the
+    encoder, every chunk inflates with zlib to the oracle's record, and the
+    image decodes on the GPU bit-exactly."""
+    from tests.helpers import parse_cz
+    eps = float(np.float32(1e-3 * (small_field.max() - small_field.min())))
+    img = cz.compress_to_image(small_field, eps, 1, 4, True, encoder="zlib")
+    info = parse_cz(bytes(img))
+    assert info["keys"]["Encoder"] == "zlib"
+    raw, roff = O.field_compress(small_field, eps, 1, 4, 1, 0, 1)
+    chunks = [c for r in info["ranks"] for c in r]
+    assert len(chunks) == len(roff) - 1
+    for i, c in enumerate(chunks):
+        assert zlib.decompress(c) == bytes(raw[roff[i]:roff[i + 1]])
+    dec = cz.decompress_image(img, 1, True)
+    assert np.array_equal(dec, O.field_decompress(raw, roff, small_field.shape, 1, 1))
+    L = O.ref(4, 1, "zlib")
+    if L is not None:  # the reference reader decodes the GPU-written file
+        with tempfile.NamedTemporaryFile(suffix=".cz") as t:
+            t.write(bytes(img))
+            t.flush()
+            assert np.array_equal(O.ref_read_cz(L, t.name, 1), dec)
