@@ -179,6 +179,42 @@ def batch_report(cz, dev, steps):
     return out
 
 
+def zlib_report(cz, f_dev, eps, steps):
+    """The same field with Encoder: zlib (GPU DEFLATE, a block per record
+    mask and byte plane): compress and decompress GB/s, size against LZ4,
+    and against zlib's default level on a sample of the same records."""
+    import torch
+    import zlib
+    stream = torch.cuda.current_stream(f_dev.device)
+    nbytes = f_dev.numel() * 4
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, r
+
+    cms, cf = timed(lambda: cz.compress_field(f_dev, eps, WTYPE, ZEROBITS, SHUFFLE, encoder="zlib"))
+    data, off = cf.to_device()
+    out = torch.empty_like(f_dev)
+    dms, _ = timed(lambda: cz.decompress_field(data, off, tuple(f_dev.shape), WTYPE, SHUFFLE, encoder="zlib",
+                                               out=out))
+    h, o = data.cpu().numpy().tobytes(), off.cpu().numpy()
+    sample = range(0, len(o) - 1, max(1, (len(o) - 1) // 64))
+    gpu = sum(int(o[c + 1] - o[c]) for c in sample)
+    ref = sum(len(zlib.compress(zlib.decompress(h[o[c]:o[c + 1]]), 6)) for c in sample)
+    return {"compress_gbs": nbytes / (cms * 1e-3) / 1e9, "decompress_gbs": nbytes / (dms * 1e-3) / 1e9,
+            "compress_ms": cms, "decompress_ms": dms, "payload_bytes": int(cf.nbytes),
+            "size_vs_zlib_level6": gpu / ref, "sample": f"{len(sample)} chunks re-compressed by zlib level 6"}
+
+
 def refit_report(cz, dev):
     """PSNR of the refit vs the plain path on the 256^3 refit field."""
     import torch
@@ -416,6 +452,9 @@ def run_ours(args, rank, world, local_rank):
 
     if rank != 0:
         return
+    zl = zlib_report(cz, f_dev, eps, max(3, min(args.steps, 20)))
+    zl["ratio"] = nbytes / zl["payload_bytes"]
+    zl["size_vs_lz4"] = zl["payload_bytes"] / comp_bytes
     refit = refit_report(cz, dev)
     batched = batch_report(cz, dev, max(3, args.steps))
     # ---- rooflines: the wavelet kernel and the LZ4 stage; the top-level
@@ -460,6 +499,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline_kernels": [roof_enc, roof_lz],
         "cpu_baseline": {"value": nbytes / cpu_s / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": sample},
+        "zlib": zl,
         "refit": refit,
         "batched": batched,
         "gpu_launches": 7 * args.steps,
