@@ -21,6 +21,8 @@ namespace cz {
 namespace zl {
 
 constexpr int kMaxBits = 15;
+constexpr int kFastBits = 10;  // codes up to this length decode with one table lookup
+constexpr int kFastMask = (1 << kFastBits) - 1;
 
 // RFC 1951 3.2.5: length codes 257..285 (li = code - 257), distance codes 0..29
 CZ_HD int len_extra(int li) { return li < 8 || li == 28 ? 0 : (li - 4) >> 2; }
@@ -57,9 +59,24 @@ struct Bits {
         over = false;
     }
     // refills to at least 57 bits (zeros past the end; reading ahead is not
-    // consuming)
+    // consuming). On the GPU, away from the end of the input, whole bytes
+    // come from three aligned 32-bit loads.
     CZ_MEM void fill()
     {
+#if defined(__CUDA_ARCH__)
+        if (pos + 12 <= end) {
+            const uintptr_t a = reinterpret_cast<uintptr_t>(p + pos);
+            const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+            const unsigned sh = (unsigned)(a & 3) * 8;
+            const unsigned long long lo = (unsigned long long)w[1] << 32 | w[0];
+            const unsigned long long v = sh ? (lo >> sh) | ((unsigned long long)w[2] << (64 - sh)) : lo;
+            const int nbytes = (64 - cnt) >> 3;
+            buf |= (nbytes == 8 ? v : (v & ((1ull << (8 * nbytes)) - 1))) << cnt;
+            pos += nbytes;
+            cnt += 8 * nbytes;
+            return;
+        }
+#endif
         while (cnt <= 56) {
             const unsigned long long b = pos < end ? p[pos] : 0ull;
             ++pos;
@@ -85,10 +102,13 @@ struct Bits {
     }
 };
 
-// Canonical code: count[len] codes of each length, symbols sorted by code.
+// Canonical code: count[len] codes of each length, symbols sorted by code,
+// and a table of the codes up to kFastBits long, indexed by the next
+// kFastBits input bits: length << 9 | symbol (0: a longer code).
 struct Huff {
     unsigned short count[kMaxBits + 1];
     unsigned short sym[288];
+    unsigned short fast[1 << kFastBits];
 };
 
 // Builds the code from lengths. Rejected as zlib rejects them: oversubscribed
@@ -112,11 +132,32 @@ CZ_HD bool build(Huff &h, const unsigned char *len, int n, bool codelen)
     for (int i = 1; i < kMaxBits; ++i) offs[i + 1] = offs[i] + h.count[i];
     for (int s = 0; s < n; ++s)
         if (len[s]) h.sym[offs[len[s]]++] = (unsigned short)s;
+    // lookup table: canonical codes in symbol order per length, bit-reversed
+    // (the stream sends codes most significant bit first)
+    for (int i = 0; i <= kFastMask; ++i) h.fast[i] = 0;
+    int next[kFastBits + 1], code = 0;
+    next[0] = 0;
+    for (int l = 1; l <= kFastBits; ++l) {
+        code = (code + h.count[l - 1]) << 1;
+        next[l] = code;
+    }
+    for (int s = 0; s < n; ++s) {
+        const int l = len[s];
+        if (!l || l > kFastBits) continue;
+        unsigned v = (unsigned)next[l]++, r = 0;
+        for (int k = 0; k < l; ++k) {
+            r = (r << 1) | (v & 1u);
+            v >>= 1;
+        }
+        for (unsigned i = r; i <= (unsigned)kFastMask; i += 1u << l) h.fast[i] = (unsigned short)(l << 9 | s);
+    }
     return true;
 }
 
-// Next symbol (codes are read most significant bit first), -1 on error.
-CZ_HD int decode(Bits &b, const Huff &h)
+// Next symbol (codes are read most significant bit first), -1 on error:
+// one table lookup for codes up to kFastBits, the canonical walk (one bit
+// per length) otherwise.
+CZ_HD int decode_slow(Bits &b, const Huff &h)
 {
     int code = 0, first = 0, index = 0;
     for (int len = 1; len <= kMaxBits; ++len) {
@@ -129,6 +170,17 @@ CZ_HD int decode(Bits &b, const Huff &h)
         code <<= 1;
     }
     return -1;
+}
+CZ_HD int decode(Bits &b, const Huff &h)
+{
+    if (b.cnt < kFastBits) b.fill();
+    const unsigned e = h.fast[b.buf & kFastMask];
+    if (!e) return decode_slow(b, h);
+    const int l = (int)(e >> 9);
+    b.buf >>= l;
+    b.cnt -= l;
+    if (8 * b.pos - b.cnt > 8 * b.end) b.over = true;
+    return (int)(e & 511);
 }
 
 // Decoder state across batches.

@@ -42,6 +42,7 @@ inflate_kernel(const uint8_t *__restrict__ in, const long long *in_off, const in
     __shared__ Huff lit, dist;
     __shared__ unsigned char lens[320];
     __shared__ int batch[kZBatch][3];  // matches: output position, length, distance
+    __shared__ int mpre[kZBatch + 1];  // exclusive prefix of the match lengths
     __shared__ int s_state[4];         // matches in the batch, error, done, Adler-32 of the trailer
     const int lane = threadIdx.x;
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
@@ -57,14 +58,49 @@ inflate_kernel(const uint8_t *__restrict__ in, const long long *in_off, const in
                 s_state[2] = z.done();
             }
             __syncwarp();
-            // the warp replays the matches in order, each byte-parallel:
-            // byte k of a match at p with distance d is out[p - d + (k mod d)]
+            // the batch's match bytes, all in parallel: byte k of a match at p
+            // with distance d is out[p - d + (k mod d)]; where that lies in an
+            // earlier match of the batch (or this one) the source is followed
+            // back until it is a byte written before the replay (a literal of
+            // the batch or earlier output)
             const int n = s_state[0];
-            for (int i = 0; i < n; ++i) {
-                const int p = batch[i][0], len = batch[i][1], d = batch[i][2];
-                for (int k = lane; k < len; k += 32) dst[p + k] = __ldcg(dst + p - d + (d >= len ? k : k % d));
-                __syncwarp();
+            {
+                int incl = 0;
+                for (int i0 = 0; i0 < n; i0 += 32) {  // exclusive prefix of the match lengths (warp-uniform loop)
+                    const int i = i0 + lane;
+                    const int v = i < n ? batch[i][1] : 0;
+                    int x = v;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int t = __shfl_up_sync(0xffffffffu, x, o);
+                        if (lane >= o) x += t;
+                    }
+                    if (i < n) mpre[i] = incl + x - v;
+                    incl += __shfl_sync(0xffffffffu, x, 31);
+                }
+                if (lane == 0) mpre[n] = incl;
             }
+            __syncwarp();
+            const int mtotal = mpre[n];
+            for (int t = lane; t < mtotal; t += 32) {
+                int i = 0;  // match holding byte t of the batch's match bytes
+#pragma unroll
+                for (int step = 64; step; step >>= 1)
+                    if (i + step < n && mpre[i + step] <= t) i += step;
+                const int y = batch[i][0] + t - mpre[i];
+                int x = y;
+                for (int hop = 0; hop <= n; ++hop) {
+                    int j = 0;  // last match starting at or before x
+#pragma unroll
+                    for (int step = 64; step; step >>= 1)
+                        if (j + step < n && batch[j + step][0] <= x) j += step;
+                    const int pj = batch[j][0], lj = batch[j][1], dj = batch[j][2];
+                    if (x < pj || x >= pj + lj) break;
+                    x = pj - dj + (dj >= lj ? x - pj : (x - pj) % dj);
+                }
+                dst[y] = __ldcg(dst + x);
+            }
+            __syncwarp();
             const int e = s_state[1], dn = s_state[2];
             __syncwarp();
             if (e || dn) break;
