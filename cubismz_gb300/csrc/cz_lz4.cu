@@ -57,6 +57,21 @@ __device__ __forceinline__ uint32_t rd32u(const uint8_t *p)
     return sh ? __funnelshift_r(w[0], w[1], sh) : w[0];
 }
 
+// 16 bytes at any byte address as four little-endian words: five aligned
+// loads, all issued before any use. May read up to 19 bytes past p (inputs
+// carry tail room).
+__device__ __forceinline__ void rd16u(const uint8_t *p, uint32_t (&v)[4])
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+    const uint32_t sh = (uint32_t)(a & 3) * 8;
+    uint32_t x[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) x[j] = w[j];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = sh ? __funnelshift_r(x[j], x[j + 1], sh) : x[j];
+}
+
 // Warp-wide copy of n bytes; 4-byte stores once dst is aligned. May read up
 // to 4 bytes past src+n (inputs carry tail room).
 __device__ __forceinline__ void warp_copy(uint8_t *dst, const uint8_t *src, int n, int lane)
@@ -71,28 +86,37 @@ __device__ __forceinline__ void warp_copy(uint8_t *dst, const uint8_t *src, int 
     const uint32_t sa = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 3);
     const uint32_t *sw = reinterpret_cast<const uint32_t *>(src - sa);
     uint32_t *dw = reinterpret_cast<uint32_t *>(dst);
-    if (sa == 0) {
-        for (int i = lane; i < nw; i += 32) dw[i] = sw[i];
-    } else {
-        for (int i = lane; i < nw; i += 32) dw[i] = __funnelshift_r(sw[i], sw[i + 1], 8 * sa);
+    // 8 words per lane in flight: every load of a round before its stores
+    constexpr int U = 8;
+    for (int i0 = 0; i0 < nw; i0 += 32 * U) {
+        uint32_t v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + 32 * u + lane;
+            v[u] = i < nw ? (sa ? __funnelshift_r(sw[i], sw[i + 1], 8 * sa) : sw[i]) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + 32 * u + lane;
+            if (i < nw) dw[i] = v[u];
+        }
     }
     const int t = n & 3;
     if (lane < t) dst[4 * nw + lane] = src[4 * nw + lane];
 }
 
-// n <= 32 bytes, 8 at a time with every load of a batch issued before its
-// stores (source and destination never overlap).
+// n <= 32 bytes: all loads (16 bytes each, aligned words) issued before any
+// store (source and destination never overlap). May read up to 35 bytes
+// past s (inputs carry tail room).
 __device__ __forceinline__ void copy_short(uint8_t *__restrict__ d, const uint8_t *__restrict__ s, int n)
 {
-#pragma unroll 1
-    for (int i = 0; i < n; i += 8) {
-        uint8_t b[8];
+    if (n <= 0) return;
+    uint32_t v[8];
+    rd16u(s, *reinterpret_cast<uint32_t(*)[4]>(v));
+    if (n > 16) rd16u(s + 16, *reinterpret_cast<uint32_t(*)[4]>(v + 4));
 #pragma unroll
-        for (int j = 0; j < 8; ++j) b[j] = i + j < n ? __ldg(s + i + j) : (uint8_t)0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (i + j < n) d[i + j] = b[j];
-    }
+    for (int i = 0; i < 32; ++i)
+        if (i < n) d[i] = (uint8_t)(v[i >> 2] >> (8 * (i & 3)));
 }
 
 // Bytes of a length field's continuation: n/255 bytes of 255, then n%255.
@@ -147,17 +171,23 @@ constexpr int kSW = 512, kSub = kSW / 32, kMaxSeqLane = kSub / 4;
 constexpr uint32_t kPosMask = (1u << 18) - 1;
 __device__ __forceinline__ uint32_t lz_tag(uint32_t v) { return (v * 0x85ebca77u) >> 18; }
 
-// exact match length from (p, cand), starting `known` bytes in (lane-local)
+// exact match length from (p, cand), starting `known` bytes in (lane-local);
+// 16 bytes per round trip to memory
 __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, int known, int matchlimit)
 {
     int len = known;
     while (p + len < matchlimit) {
-        const uint32_t x = rd32u(src + p + len) ^ rd32u(src + cand + len);
-        if (x) {
-            len += (__ffs(x) - 1) >> 3;
-            break;
+        uint32_t a[4], b[4];
+        rd16u(src + p + len, a);
+        rd16u(src + cand + len, b);
+        int k = 16;
+#pragma unroll
+        for (int j = 3; j >= 0; --j) {
+            const uint32_t x = a[j] ^ b[j];
+            if (x) k = 4 * j + ((__ffs(x) - 1) >> 3);
         }
-        len += 4;
+        len += k;
+        if (k < 16) break;
     }
     return len < matchlimit - p ? len : matchlimit - p;
 }
@@ -166,25 +196,31 @@ __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, in
 // to 32 KiB, and per kept sequence one 8-byte record (literal run, match
 // length, distance; zl::seq_pack) at out + out_off[c]; the last record holds
 // the tail literals. out_len[c] = record bytes, -1 past the capacity.
+// Shared memory of one encoder warp (dynamic shared memory, one per warp).
+struct LzEncWarp {
+    uint32_t table[1 << kHashLog];
+    int4 longq[32];                   // (dst offset, src offset, n, -)
+    uint32_t seq[32][kMaxSeqLane];    // start - base | offset << 16
+    int lens[32][kMaxSeqLane];
+    uint16_t info[kSW];               // candidate offset per position, 0: none
+    int nlong;
+};
+
 template <int kLzWarps, bool SEQ>
 __global__ void __launch_bounds__(kLzWarps * 32)
 lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
                   uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records)
 {
     constexpr int kMaxOff = SEQ ? zl::kMaxDist : 65535;
-    __shared__ uint32_t table_all[kLzWarps][1 << kHashLog];
-    __shared__ uint16_t info_all[kLzWarps][kSW];                // candidate offset per position, 0: none
-    __shared__ uint32_t seq_all[kLzWarps][32][kMaxSeqLane];     // start - base | offset << 16
-    __shared__ int lens_all[kLzWarps][32][kMaxSeqLane];
-    __shared__ int4 longq_all[kLzWarps][32];  // (dst offset, src offset, n, -)
-    __shared__ int nlong_all[kLzWarps];
+    extern __shared__ __align__(16) unsigned char lz_enc_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    uint32_t *table = table_all[wib];
-    uint16_t *info = info_all[wib];
-    uint32_t *myseq = seq_all[wib][lane];
-    int *mylen = lens_all[wib][lane];
-    int4 *longq = longq_all[wib];
-    int &nlong = nlong_all[wib];
+    LzEncWarp &ws = reinterpret_cast<LzEncWarp *>(lz_enc_smem)[wib];
+    uint32_t *table = ws.table;
+    uint16_t *info = ws.info;
+    uint32_t *myseq = ws.seq[lane];
+    int *mylen = ws.lens[lane];
+    int4 *longq = ws.longq;
+    int &nlong = ws.nlong;
     const int gw = blockIdx.x * kLzWarps + wib, nw = gridDim.x * kLzWarps;
 
     for (int c = gw; c < nchunks; c += nw) {
@@ -825,17 +861,35 @@ __global__ void gather_kernel(const uint8_t *__restrict__ src, const long long *
 
 using namespace cz;
 
+// kLzWarps chunks per CTA; 32 fills an SM (1024 threads, ~210 KB of shared
+// memory), so that CTAs of this kernel and the wavelet kernel, which also
+// takes a whole SM, share the machine SM by SM.
+template <int W, bool SEQ>
+static cudaError_t launch_enc(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
+                              uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
+                              cudaStream_t st)
+{
+    const int sm = (int)sizeof(LzEncWarp) * W;
+    auto k = lz4_encode_kernel<W, SEQ>;
+    if (sm > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        if (e != cudaSuccess) return e;
+    }
+    k<<<grid, W * 32, sm, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records);
+    return cudaGetLastError();
+}
+
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
                                  int grid, cudaStream_t st)
 {
     if (nchunks <= 0) return cudaSuccess;
     switch (warps) {
-    case 2: lz4_encode_kernel<2, false><<<grid, 64, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records); break;
-    case 8: lz4_encode_kernel<8, false><<<grid, 256, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records); break;
-    default: lz4_encode_kernel<4, false><<<grid, 128, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records);
+    case 2: return launch_enc<2, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
+    case 8: return launch_enc<8, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
+    case 32: return launch_enc<32, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
+    default: return launch_enc<4, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
     }
-    return cudaGetLastError();
 }
 
 cudaError_t cz_launch_lz77_parse(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
@@ -843,8 +897,7 @@ cudaError_t cz_launch_lz77_parse(const uint8_t *in, const long long *in_off, con
                                  cudaStream_t st)
 {
     if (nchunks <= 0) return cudaSuccess;
-    lz4_encode_kernel<4, true><<<grid, 128, 0, st>>>(in, in_off, in_len, nchunks, seq, seq_off, seq_bytes, records);
-    return cudaGetLastError();
+    return launch_enc<4, true>(in, in_off, in_len, nchunks, seq, seq_off, seq_bytes, records, grid, st);
 }
 
 cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
