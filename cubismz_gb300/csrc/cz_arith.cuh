@@ -152,12 +152,24 @@ CZ_HD void split(const float (&v)[H], float C, float (&hi)[H], float (&lo)[H])
 
 // Line-level analysis and split on the main grid. Returns true when the
 // binary32 fast path is exact for every stencil with K <= 32 on this line.
+// One pass gives the largest magnitude and the smallest non-zero one (as
+// bits - 1, unsigned, so that zeros never count); the spread test of
+// `within` is then one compare.
 template <int H>
 CZ_HD bool line_split(const float (&v)[H], float (&hi)[H], float (&lo)[H], uint32_t &amax)
 {
-    amax = max_bits<H>(v);
-    split<H>(v, split_const<kGridBits>(amax), hi, lo);
-    return within<H>(v, amax, kSpread);
+    uint32_t mx = 0, mn1 = 0xffffffffu;
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+        const uint32_t m = CZ_BITS(v[i]) & 0x7fffffffu;
+        mx = CZ_UMAX(mx, m);
+        mn1 = CZ_UMIN(mn1, m - 1u);
+    }
+    amax = mx;
+    split<H>(v, split_const<kGridBits>(mx), hi, lo);
+    const uint32_t eb = mx >> 23;
+    const uint32_t tb = ((eb - (uint32_t)kSpread) << 23) - 1u;
+    return (mx == 0u) || (eb >= 27u && eb <= 247u && mn1 >= tb);
 }
 
 // RN32 of sum c_i*(hi_i+lo_i) given an exact split (see header).

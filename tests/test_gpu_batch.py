@@ -48,3 +48,27 @@ def test_plan_graph_batch(cz):
     fields[2] = fields[2] * np.float32(2.0)
     check(fields)
     plan.close()
+
+
+def test_plan_with_zlib_encoder(cz):
+    """A plan with Encoder: zlib: every field's chunks inflate with zlib to
+    the oracle's records, and the fields decode bit-exactly on the GPU."""
+    import zlib
+    import torch
+    from cubismz_gb300 import synth
+    fields = [synth.generate(s, seed=10 + i, blobs=6, interfaces=2) for i, s in enumerate(SHAPES)]
+    eps = [float(np.float32(t * (f.max() - f.min()))) for t, f in zip(THR, fields)]
+    dev = [torch.from_numpy(f).cuda() for f in fields]
+    plan = cz.Plan(dev, eps, wtype=1, zerobits=4, shuffle=True, encoder="zlib", tune=True)
+    plan.launch()
+    cf = plan.result()
+    data, off = cf.to_device()
+    for i, f in enumerate(fields):
+        d, o = plan.field_chunks(data, off, i)
+        hd, ho = d.cpu().numpy().tobytes(), o.cpu().numpy()
+        raw, roff = O.field_compress(f, eps[i], 1, 4, 1, 0, 1)
+        for c in range(len(ho) - 1):
+            assert zlib.decompress(hd[ho[c]:ho[c + 1]]) == bytes(raw[roff[c]:roff[c + 1]])
+        dec = cz.decompress_field(d, o, f.shape, 1, True, encoder="zlib").cpu().numpy()
+        assert np.array_equal(dec, O.field_decompress(raw, roff, f.shape, 1, 1))
+    plan.close()

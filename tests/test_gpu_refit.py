@@ -150,3 +150,27 @@ def test_refit_keeps_mask_and_raises_psnr(cz, small_field, zb, shuffle, encoder)
     # survivors' byte planes a little less tightly
     ratio_p, ratio_r = small_field.nbytes / plain.nbytes, small_field.nbytes / refit.nbytes
     assert abs(ratio_r / ratio_p - 1) < 0.05
+
+
+def test_refit_with_zlib_encoder(cz, small_field):
+    """Refit streams with Encoder: zlib: every chunk inflates with zlib to a
+    record with the plain path's mask, the restated reference decoder reads
+    the inflated records to the GPU's decode, and the refit PSNR is higher."""
+    import zlib
+    import torch
+    f = torch.from_numpy(small_field).cuda()
+    eps = float(np.float32(1e-3 * (small_field.max() - small_field.min())))
+    raw, roff = O.field_compress(small_field, eps, 1, 4, 1, 0, 1)
+    refit = cz.refit_field(f, eps, iters=20, wtype=1, zerobits=4, shuffle=True, encoder="zlib")
+    rd, ro = refit.to_device()
+    hd, ho = rd.cpu().numpy().tobytes(), ro.cpu().numpy()
+    recs = [zlib.decompress(hd[ho[c]:ho[c + 1]]) for c in range(len(ho) - 1)]
+    for c, r in enumerate(recs):
+        want = bytes(raw[roff[c]:roff[c + 1]])
+        assert len(r) == len(want) and r[:4 + 4096] == want[:4 + 4096]  # header and mask
+    rec_off = np.concatenate([[0], np.cumsum([len(r) for r in recs])]).astype(np.int64)
+    ref = O.field_decompress(np.frombuffer(b"".join(recs), np.uint8), rec_off, small_field.shape, 1, 1)
+    dec = cz.decompress_field(rd, ro, small_field.shape, 1, True, encoder="zlib").cpu().numpy()
+    assert np.array_equal(ref, dec)
+    plain = O.field_decompress(raw, roff, small_field.shape, 1, 1)
+    assert _psnr(small_field, dec) > _psnr(small_field, plain) + 0.1
