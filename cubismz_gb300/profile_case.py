@@ -1,14 +1,20 @@
 """Profiling case for the codec kernels: a 256x512x512 fp32 field (256 MiB,
 larger than L2; 60 blobs, 6 interfaces, seed 3), compressed three times with
-wtype 1, threshold 1e-3 x range, zerobits 4, shuffle and LZ4, then
-decompressed twice. Prints the per-stage device times of each call.
+wtype 1, threshold 1e-3 x range, zerobits 4, shuffle and the chosen lossless
+stage (LZ4 by default, or zlib), then decompressed twice. Prints the
+per-stage device times of each call.
 
-    python -m cubismz_gb300.profile_case
+    python -m cubismz_gb300.profile_case [--encoder lz4|zlib]
 """
+import argparse
+
 import numpy as np
 
 
 def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--encoder", default="lz4", choices=["lz4", "zlib"])
+    enc = ap.parse_args().encoder
     import torch
     import cubismz_gb300 as cz
     from cubismz_gb300 import synth
@@ -19,13 +25,13 @@ def main():
     ctx = cz.context(0)
     ctx.set_timing(True)
     for _ in range(3):
-        cf = cz.compress_field(f, eps, 1, 4, True, encoder="lz4")
-        print("compress stages ms (encode, lz4, assembly):", ctx.stage_times(), "raw", cf.raw_bytes,
+        cf = cz.compress_field(f, eps, 1, 4, True, encoder=enc)
+        print(f"compress stages ms (encode, {enc}, assembly):", ctx.stage_times(), "raw", cf.raw_bytes,
               "payload", cf.nbytes)
     data, off = cf.to_device()
     for _ in range(2):
-        cz.decompress_field(data, off, shape, 1, True, encoder="lz4")
-        print("decompress stages ms (lz4, locate, decode):", ctx.stage_times())
+        cz.decompress_field(data, off, shape, 1, True, encoder=enc)
+        print(f"decompress stages ms ({enc}, locate, decode):", ctx.stage_times())
     torch.cuda.synchronize()
 
 
