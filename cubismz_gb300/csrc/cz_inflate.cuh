@@ -307,6 +307,22 @@ struct Inflater {
                 in_block = 0;
                 continue;
             }
+            // literals while at least 8 input and 8 output bytes remain: one
+            // table lookup each and no per-symbol end tests (a refill then
+            // stays within the input, a literal within the output); other
+            // symbols and long codes take the general path below
+            {
+                const long long olim = oend - 8, ilim = b.end - 8;
+                while (op <= olim && b.pos <= ilim) {
+                    if (b.cnt < kFastBits) b.fill();
+                    const unsigned e = lit.fast[b.buf & kFastMask];
+                    if (!e || (e & 511u) >= 256u) break;
+                    const int l = (int)(e >> 9);
+                    b.buf >>= l;
+                    b.cnt -= l;
+                    dst[op++] = (uint8_t)e;
+                }
+            }
             const int sym = decode(b, lit);
             if (sym < 0 || b.over) {
                 err = 14;
