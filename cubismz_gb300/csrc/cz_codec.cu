@@ -131,16 +131,6 @@ encode_kernel(const CzField *fields, int nfields, long long total_blocks, int ze
     encode_body<KIND>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
 }
 
-// The same with at most 120 registers per thread: leaves room on the SM for
-// a 2-warp LZ4 CTA, so that pipelined stages run side by side.
-template <int KIND>
-__global__ void __maxnreg__(120)
-encode_kernel_lean(const CzField *fields, int nfields, long long total_blocks, int zerobits, int shuffle,
-                   uint8_t *stage, int *rec_bytes, unsigned long long *queue)
-{
-    encode_body<KIND>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
-}
-
 // Error statistics of a decoded block against a reference field (the
 // quantities of cz2diff, Tools/cz2diff.cpp:116-261): per block
 // {e_inf, n_inf, e_1, n_1, e_2, n_2, min, max} with e = |decoded - ref|,
@@ -374,9 +364,9 @@ extern "C" int cz_codec_smem_bytes(void) { return kSmBytes; }
 template <int KIND>
 static cudaError_t launch_encode(const CzField *fields, int nfields, long long total_blocks, int zerobits,
                                  int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
-                                 cudaStream_t st, bool lean)
+                                 cudaStream_t st)
 {
-    auto k = lean ? encode_kernel_lean<KIND> : encode_kernel<KIND>;
+    auto k = encode_kernel<KIND>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
     if (e != cudaSuccess) return e;
     k<<<grid, kNT, kSmBytes, st>>>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
@@ -399,18 +389,15 @@ static cudaError_t launch_decode(const CzField *fields, int nfields, long long t
 
 cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long long total_blocks, int zerobits,
                              int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
-                             cudaStream_t st, int lean)
+                             cudaStream_t st)
 {
     switch (wkind(wtype)) {
     case 1:
-        return launch_encode<1>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
-                                lean != 0);
+        return launch_encode<1>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
     case 2:
-        return launch_encode<2>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
-                                lean != 0);
+        return launch_encode<2>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
     default:
-        return launch_encode<3>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
-                                lean != 0);
+        return launch_encode<3>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
     }
 }
 
