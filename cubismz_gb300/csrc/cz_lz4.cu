@@ -212,9 +212,11 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                   uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records)
 {
     constexpr int kMaxOff = SEQ ? zl::kMaxDist : 65535;
+    // up to 8 warps in static shared memory; 32 (a whole SM) in dynamic
     extern __shared__ __align__(16) unsigned char lz_enc_smem[];
+    __shared__ LzEncWarp lz_enc_static[kLzWarps <= 8 ? kLzWarps : 1];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    LzEncWarp &ws = reinterpret_cast<LzEncWarp *>(lz_enc_smem)[wib];
+    LzEncWarp &ws = (kLzWarps <= 8 ? lz_enc_static : reinterpret_cast<LzEncWarp *>(lz_enc_smem))[wib];
     uint32_t *table = ws.table;
     uint16_t *info = ws.info;
     uint32_t *myseq = ws.seq[lane];
@@ -869,7 +871,7 @@ static cudaError_t launch_enc(const uint8_t *in, const long long *in_off, const 
                               uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
                               cudaStream_t st)
 {
-    const int sm = (int)sizeof(LzEncWarp) * W;
+    const int sm = W <= 8 ? 0 : (int)sizeof(LzEncWarp) * W;
     auto k = lz4_encode_kernel<W, SEQ>;
     if (sm > 48 * 1024) {
         const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
