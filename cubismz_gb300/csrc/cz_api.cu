@@ -47,7 +47,7 @@ struct cz_ctx {
     std::string err;
     DevBuf fields, stage, rec_bytes, chunk_in, in_off, in_len, blk_dst, lz_off, lz_out, lz_len, out_off, out_data,
         queue, status, flag, rec_off, dec, dec_off, dec_cap, dec_len, raw_off, chunk_rec, block_chunk, block_subid,
-        tmp_field, tmp_in, refit, diff, zout, zoff, zlen;
+        tmp_field, tmp_in, refit, diff, zout, zoff, zlen, ierr;
     void *pin = nullptr;  // small pinned host scratch
     size_t pin_cap = 0;
     // geometry of the last compressed stream
@@ -443,7 +443,7 @@ int cz_destroy(cz_ctx *c)
 {
     if (!c) return CZ_OK;
     cudaSetDevice(c->device);
-    DevBuf *all[] = {&c->zout, &c->zoff, &c->zlen, &c->diff, &c->refit, &c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
+    DevBuf *all[] = {&c->ierr, &c->zout, &c->zoff, &c->zlen, &c->diff, &c->refit, &c->fields,  &c->stage,   &c->rec_bytes, &c->chunk_in,  &c->in_off,      &c->in_len,
                      &c->blk_dst, &c->lz_off,  &c->lz_out,    &c->lz_len,    &c->out_off,     &c->out_data,
                      &c->queue,   &c->status,  &c->flag,      &c->rec_off,   &c->dec,         &c->dec_off,
                      &c->dec_cap, &c->dec_len, &c->raw_off,   &c->chunk_rec, &c->block_chunk, &c->block_subid,
@@ -606,6 +606,18 @@ int cz_res_line(const double *st, long long compressed_bytes, char *buf, int len
     return w < len ? CZ_OK : CZ_E_SPACE;
 }
 
+// After a TMA transpose: the kernel's error flag (a bounded mbarrier wait
+// that ran out); waits for the stream.
+static int ingest_check(cz_ctx *c, cudaStream_t st)
+{
+    CZ_TRY(grow_pin(c, 4096));
+    int *h = reinterpret_cast<int *>(c->pin);
+    CZ_CUDA(c, cudaMemcpyAsync(h, c->ierr.p, 4, cudaMemcpyDeviceToHost, st));
+    CZ_CUDA(c, cudaStreamSynchronize(st));
+    if (*h != 0) return fail(c, CZ_E_CUDA, "layout transform: a tile copy did not complete");
+    return CZ_OK;
+}
+
 int cz_field_from_zfastest(cz_ctx *c, const void *d_in, int bytes, int nch, int ch, int nx, int ny, int nz,
                            float *d_field, void *stream)
 {
@@ -613,8 +625,12 @@ int cz_field_from_zfastest(cz_ctx *c, const void *d_in, int bytes, int nch, int 
         nz < 1 || ny > 65535)
         return fail(c, CZ_E_ARG, "bad layout arguments");
     CZ_TRY(set_device(c));
-    CZ_CUDA(c, cz_launch_from_zfastest(d_in, bytes, nch, ch, nx, ny, nz, d_field, (cudaStream_t)stream));
-    return CZ_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    CZ_TRY(grow(c, c->ierr, 64));
+    CZ_CUDA(c, cudaMemsetAsync(c->ierr.p, 0, 4, st));
+    bool tma = false;
+    CZ_CUDA(c, cz_launch_from_zfastest(d_in, bytes, nch, ch, nx, ny, nz, d_field, st, P<int>(c->ierr), &tma));
+    return tma ? ingest_check(c, st) : CZ_OK;
 }
 
 int cz_field_to_zfastest(cz_ctx *c, const float *d_field, int nx, int ny, int nz, int nch, int ch, float *d_out,
@@ -623,8 +639,12 @@ int cz_field_to_zfastest(cz_ctx *c, const float *d_field, int nx, int ny, int nz
     if (!c || !d_field || !d_out || nch < 1 || ch < 0 || ch >= nch || nx < 1 || ny < 1 || nz < 1 || ny > 65535)
         return fail(c, CZ_E_ARG, "bad layout arguments");
     CZ_TRY(set_device(c));
-    CZ_CUDA(c, cz_launch_to_zfastest(d_field, nx, ny, nz, nch, ch, d_out, (cudaStream_t)stream));
-    return CZ_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    CZ_TRY(grow(c, c->ierr, 64));
+    CZ_CUDA(c, cudaMemsetAsync(c->ierr.p, 0, 4, st));
+    bool tma = false;
+    CZ_CUDA(c, cz_launch_to_zfastest(d_field, nx, ny, nz, nch, ch, d_out, st, P<int>(c->ierr), &tma));
+    return tma ? ingest_check(c, st) : CZ_OK;
 }
 
 int cz_batch_compress(cz_ctx *c, int nfields, const float *const *d_fields, const int *dims, const float *eps,

@@ -106,9 +106,11 @@ cudaError_t cz_launch_rebase(long long *off, int n, long long base, cudaStream_t
 // Layout of the reference's HDF5 tools (cz_ingest.cu): z-fastest arrays with
 // interleaved channels <-> the x-fastest field. bytes: 4 (float) or 8 (double).
 cudaError_t cz_launch_from_zfastest(const void *in, int bytes, int nch, int ch, int nx, int ny, int nz, float *out,
-                                    cudaStream_t st);
+                                    cudaStream_t st, int *err = nullptr,
+                                    bool *used_tma = nullptr);
 cudaError_t cz_launch_to_zfastest(const float *in, int nx, int ny, int nz, int nch, int ch, float *out,
-                                  cudaStream_t st);
+                                  cudaStream_t st, int *err = nullptr,
+                                  bool *used_tma = nullptr);
 
 // zlib streams (cz_zlib.cu): one warp per chunk; out_len[c] = bytes or < 0.
 cudaError_t cz_launch_inflate(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks, uint8_t *out,

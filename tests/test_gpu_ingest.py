@@ -33,6 +33,22 @@ def test_zfastest_roundtrip(cz, dtype, nch, ch):
         assert torch.count_nonzero(out[..., others]) == 0
 
 
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+@pytest.mark.parametrize("shape", [(96, 40, 64), (32, 1, 32), (256, 7, 160)])
+def test_zfastest_tiled_path(cz, dtype, shape):
+    """Single-channel arrays with tile-multiple extents (the TMA tile path):
+    both directions exact, every element placed once."""
+    import torch
+    nx, ny, nz = shape
+    g = torch.Generator(device="cuda").manual_seed(11)
+    arr = torch.randn(shape, generator=g, device="cuda", dtype=getattr(torch, dtype))
+    f = cz.field_from_zfastest(arr)
+    assert torch.equal(f, arr.permute(2, 1, 0).contiguous().float())
+    out = torch.full(shape, float("nan"), device="cuda", dtype=torch.float32)
+    cz.field_to_zfastest(f, out=out)
+    assert torch.equal(out, arr.float())
+
+
 def test_ingest_compress_egress(cz, small_field):
     """hdf2cz -> codec -> cz2hdf: the z-fastest array survives up to the
     codec's error, and equals the x-fastest path's decode."""
