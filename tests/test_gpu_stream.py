@@ -92,3 +92,22 @@ def test_fused_decode_and_error_norms(cz, small_field):
     for k in ("e_1", "n_1", "e_2", "n_2"):
         assert abs(got[k] - want[k]) <= 1e-12 * abs(want[k]), k
     assert got["res_line"] == cz.res_line(want, cf.nbytes)
+
+
+@pytest.mark.parametrize("encoder", ["lz4", "zlib"])
+def test_all_coefficients_kept(cz, small_field, encoder):
+    """A negative threshold keeps every coefficient: records of the maximum
+    size (4 + 4096 + 4*32768 bytes) with byte planes close to
+    incompressible. Both lossless stages round-trip them through the field
+    and the pipelined image paths, bit-exactly to the oracle."""
+    import torch
+    field = np.ascontiguousarray(small_field[:64])
+    raw, roff = O.field_compress(field, -1.0, 1, 0, 1, 0, 1)
+    assert set(np.diff(roff).tolist()) == {4 + 4096 + 4 * 32768}
+    want = O.field_decompress(raw, roff, field.shape, 1, 1)
+    cf = cz.compress_field(torch.from_numpy(field).cuda(), -1.0, 1, 0, True, encoder=encoder)
+    data, off = cf.to_device()
+    dec = cz.decompress_field(data, off, field.shape, 1, True, encoder=encoder).cpu().numpy()
+    assert np.array_equal(dec.view(np.uint32), want.view(np.uint32))
+    img = cz.compress_to_image(field, -1.0, 1, 0, True, encoder=encoder)
+    assert np.array_equal(cz.decompress_image(img, 1, True).view(np.uint32), want.view(np.uint32))
