@@ -143,12 +143,17 @@ CZ_HD void canon_codes(const uint8_t *len, int n, uint16_t *code)
             code[s] = 0;
             continue;
         }
-        unsigned v = (unsigned)next[l]++, r = 0;
+        unsigned v = (unsigned)next[l]++;
+#if defined(__CUDA_ARCH__)
+        code[s] = (uint16_t)(__brev(v) >> (32 - l));
+#else
+        unsigned r = 0;
         for (int k = 0; k < l; ++k) {
             r = (r << 1) | (v & 1u);
             v >>= 1;
         }
         code[s] = (uint16_t)r;
+#endif
     }
 }
 

@@ -147,7 +147,8 @@ struct DeflateWarp {
     union {
         uint32_t ring[kRingW];
         struct {  // code construction
-            uint32_t wt[288], w[288], iw[288];
+            uint32_t key[512];  // (weight << 9 | symbol), sorted; unused: ~0
+            uint32_t w[288], iw[288];
             uint16_t sym[288], par[576], dep[576];
             uint8_t l[288];
         } b;
@@ -156,37 +157,50 @@ struct DeflateWarp {
     int state[4];
 };
 
-// Code lengths for freq[0..n) into len (the warp ranks the used symbols by
-// (frequency, symbol), lane 0 runs huff_lengths). False if it fails.
+// Code lengths for freq[0..n) into len: the warp sorts the used symbols by
+// (frequency, symbol) -- a bitonic sort of keys weight << 9 | symbol over 512
+// slots (block counts stay below 2^22) -- and lane 0 runs huff_lengths.
+// False if it fails.
 __device__ bool warp_code(DeflateWarp &s, const uint32_t *freq, int n, uint8_t *len, int lane)
 {
     auto &b = s.u.b;
     int used = 0;
-    for (int x = lane; x < n; x += 32) {
-        b.wt[x] = freq[x];
-        used += freq[x] != 0;
-    }
+    for (int x = lane; x < n; x += 32) used += freq[x] != 0;
 #pragma unroll
     for (int o = 16; o; o >>= 1) used += __shfl_xor_sync(0xffffffffu, used, o);
+    // at least two codes: the lowest unused symbols get weight one (never sent)
+    int need = used < 2 ? 2 - used : 0;
+    for (int x0 = 0; x0 < 512; x0 += 32) {
+        const int x = x0 + lane;
+        uint32_t f = x < n ? freq[x] : 0u;
+        const bool zero = x < n && f == 0u;
+        const unsigned zb = __ballot_sync(0xffffffffu, zero);
+        if (zero && need > 0 && __popc(zb & ((1u << lane) - 1u)) < need) f = 1u;
+        need -= min(need, __popc(zb));
+        b.key[x] = f ? (f << 9 | (uint32_t)x) : 0xffffffffu;
+    }
+    used = max(used, 2);
     __syncwarp();
-    if (lane == 0)  // at least two codes: dummies of weight one, never sent
-        for (int x = 0; used < 2 && x < n; ++x)
-            if (!b.wt[x]) {
-                b.wt[x] = 1;
-                ++used;
+    // bitonic sort, ascending, 256 compare-exchanges per pass
+    for (int k = 2; k <= 512; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < 256; i += 32) {
+                const int lo = ((i & ~(j - 1)) << 1) | (i & (j - 1)), hi = lo + j;
+                const uint32_t a = b.key[lo], c = b.key[hi];
+                const bool up = (lo & k) == 0;
+                if ((a > c) == up) {
+                    b.key[lo] = c;
+                    b.key[hi] = a;
+                }
             }
-    __syncwarp();
-    for (int x = lane; x < n; x += 32) {
-        len[x] = 0;
-        const uint32_t wx = b.wt[x];
-        if (!wx) continue;
-        int r = 0;
-        for (int y = 0; y < n; ++y) {
-            const uint32_t wy = b.wt[y];
-            r += wy && (wy < wx || (wy == wx && y < x));
+            __syncwarp();
         }
-        b.sym[r] = (uint16_t)x;
-        b.w[r] = wx;
+    }
+    for (int x = lane; x < n; x += 32) len[x] = 0;
+    for (int r = lane; r < used; r += 32) {
+        const uint32_t kk = b.key[r];
+        b.sym[r] = (uint16_t)(kk & 511u);
+        b.w[r] = kk >> 9;
     }
     __syncwarp();
     int ok = 1;
