@@ -3,33 +3,32 @@
 // Encoder: greedy parse, format-compatible with the reference decoder
 // LZ4_uncompress_unknownOutputSize (ThirdParty/lz4/lz4.c:802-905): minimum
 // match 4, offsets 1..65535, the last 5 bytes are literals and the last
-// match starts at least 12 bytes before the end (lz4.c:177-204).
-//   * Probe: a warp takes a 128-position window per step. Every lane loads
-//     one aligned word (coalesced), takes the next word from its neighbour
-//     and forms the 4-byte sequences of its 4 positions. The hash table
-//     (2 Ki entries per warp, shared memory) stores position and sequence,
-//     so candidates are verified without memory reads; repeats inside the
-//     window are paired with __match_any_sync. Each lane then measures the
-//     match length of its own candidates (up to 32 bytes; longer ones are
-//     finished cooperatively when chosen).
-//   * Select: the greedy walk through the window -- lowest position at or
-//     after the cursor that has a match, take it, jump past it -- costs one
-//     ballot per sequence; the window is never probed twice.
-//   * Emit: sequences collect in a shared-memory batch; a flush sizes them
-//     with a warp scan and lets every lane write one sequence (token,
-//     lengths, short literals, offset); long literal runs are copied by the
-//     whole warp.
-//   * Windows without a match advance faster after 8 misses (the reference's
-//     acceleration idea, lz4.c:389-393). Chunks made of block records
-//     ([int32 nbytes][mask][4 byte planes], shuffle on) skip the search over
-//     byte planes 1 and 2 -- the two middle mantissa bytes, which do not
-//     compress -- and copy them as literals.
+// match starts at least 12 bytes before the end (lz4.c:177-204). A warp
+// takes super-windows of 512 positions:
+//   * probe  -- 4 positions per lane per step from coalesced word loads; a
+//     hash table of 1024 entries per warp in shared memory holds position
+//     (mod 2^18) and a 14-bit tag of the 4-byte sequence, so most false
+//     candidates are dropped without reading memory;
+//   * walk   -- lane k parses positions [32k, 32k+32) greedily, measuring
+//     matches against memory 16 bytes per round trip;
+//   * merge  -- lane k keeps the sequences that start at or after the end
+//     of the last kept match of lanes < k (one ballot when no match crosses
+//     a later lane's last start, the exact serial rule otherwise);
+//   * emit   -- a warp scan places every kept sequence, each lane writes its
+//     own; literal runs over 32 bytes are copied by the whole warp.
+// Windows without a match advance faster after repeated misses (the
+// reference's acceleration idea, lz4.c:389-393). Chunks of block records
+// ([int32 nbytes][mask][4 byte planes], shuffle on) skip the search over
+// byte planes 1 and 2 -- the two middle mantissa bytes, which do not
+// compress -- and copy them as literals. The same parse in SEQ mode feeds
+// the DEFLATE encoder (cz_zlib.cu).
 // Decoder: the same acceptance tests and error convention as
 // LZ4_uncompress_unknownOutputSize (-(input position) on malformed input; an
-// empty input yields 0). A walk over the tokens records a batch of
-// sequences; literals of the batch are then copied in parallel and matches
-// replayed in order, each by the whole warp (overlapping matches repeat
-// their first `offset` bytes, the byte-serial copy semantics).
+// empty input yields 0). Windows of 128 input bytes are parsed
+// speculatively (every lane decodes tokens at 4 candidate positions; jump
+// tables by pointer doubling find the real sequences), output is staged in a
+// 4 KB per-warp ring and flushed with word stores; overlapping matches
+// repeat their first `offset` bytes, the byte-serial copy semantics.
 #include "cz_codec.h"
 #include "cz_deflate.cuh"
 

@@ -4,28 +4,28 @@
 // CompressionEncoders.h:48-88).
 //
 // Encoder (deflate_kernel): one warp per chunk, fed by the LZ77 parse of the
-// LZ4 encoder run with a 32 KiB window (cz_lz4.cu, SEQ mode). Pass 1 counts
-// the symbols (literal bytes with one shared-memory add per distinct byte
-// of 32; matches of more than 258 bytes in pieces) and sums the Adler-32;
-// the codes follow (symbols ranked by the warp, lengths limited to 15 bits
-// by one lane, cz_deflate.cuh); the exact sizes of the stored, fixed and
-// dynamic codings pick the smallest; pass 2 writes the block: 32 items per
+// LZ4 encoder run with a 32 KiB window (cz_lz4.cu, SEQ mode). A chunk of
+// shuffled block records gets a DEFLATE block per record mask and byte
+// plane (other chunks one per 64 KiB): per block, the warp counts the
+// symbols of the items that start in it (literal bytes with one
+// shared-memory add per distinct byte of 32; matches of more than 258 bytes
+// in pieces), sorts the used symbols (bitonic, by frequency), one lane
+// builds the length-limited codes (cz_deflate.cuh), and the exact sizes of
+// the stored, fixed and dynamic codings pick the smallest; then 32 items per
 // step (a literal or a match piece each), a warp scan of their bit counts,
 // and OR-writes into a per-warp ring of words that is flushed to the output
-// with word stores. One block per chunk (BFINAL set), zlib header 78 9C.
+// with word stores. zlib header 78 9C, Adler-32 by a warp reduction.
 //
-// Decoder: one warp per chunk. Lane 0 reads the header and the blocks
-// (stored, fixed Huffman, dynamic Huffman) and decodes symbols with the
-// canonical codes (per code length: count and first symbol, so a symbol
-// costs one bit test per code length); it records a batch of sequences
-// (literal run from the output it wrote, match length, distance). The warp
-// then copies the batch's matches in order, each byte-parallel: byte k of a
-// match at p with distance d is out[p - d + (k mod d)], always already
-// written. The Adler-32 of the output is a warp reduction, checked against
-// the trailer. Malformed input (bad header, code lengths, symbols,
-// distances past the start, output past the capacity, truncated input or a
-// wrong checksum) gives a negative length; every read and write is bounds
-// checked.
+// Decoder (inflate_kernel): one warp per chunk. Lane 0 reads the header and
+// the blocks (stored, fixed Huffman, dynamic Huffman) and decodes symbols
+// with 10-bit lookup tables (longer codes by the canonical walk); literals
+// go straight to the output, matches into a batch. The warp then writes all
+// of the batch's match bytes in parallel, each following its source back
+// through earlier matches of the batch to a byte written before. The Adler-32
+// of the output is a warp reduction, checked against the trailer. Malformed
+// input (bad header, code lengths, symbols, distances past the start, output
+// past the capacity, truncated input or a wrong checksum) gives a negative
+// length; every read and write is bounds checked.
 #include "cz_codec.h"
 #include "cz_deflate.cuh"
 
