@@ -6,10 +6,13 @@
 //   chunk_setup          chunk geometry (blocks_per_chunk records per chunk)
 //   pack_records         (blocks_per_chunk > 1) records back to back per chunk
 //   lz4_encode_kernel    (encoder lz4) one warp per chunk
+//   lz77 parse, deflate  (encoder zlib) one warp per chunk each
 //   scan                 chunk offsets (replaces the writer's offset allocation)
 //   gather               chunk payloads back to back
-// Decompress pipeline: decode_setup, lz4_decode_kernel, record location,
-// decode_kernel (load + iwt) straight into the output field.
+// Decompress pipeline: decode_setup, lz4_decode_kernel or inflate_kernel,
+// record location, decode_kernel (load + iwt, optionally cz2diff's error
+// sums) straight into the output field. cz_compress_to_image pipelines the
+// compress steps over z-slabs behind the host-to-device copies.
 #include <cuda_runtime.h>
 
 #include <cstdio>
