@@ -202,6 +202,61 @@ struct Inflater {
         if ((cmf & 15) != 8 || (cmf >> 4) > 7 || ((cmf << 8) | flg) % 31 || (flg & 32)) err = 1;
     }
 
+    // Reads a block header at the current position (BFINAL, BTYPE; LEN/NLEN
+    // of a stored block; the code tables of a Huffman block, built into lit
+    // and dist). Returns err (0: the block's data follows).
+    CZ_MEM int block_header(Huff &lit, Huff &dist, unsigned char *lens)
+    {
+        final_block = (int)b.get(1);
+        btype = (int)b.get(2);
+        in_block = 1;
+        if (btype == 0) {
+            b.align();
+            const unsigned l = b.get(16), nl = b.get(16);
+            if ((l ^ 0xffffu) != nl || b.over) return err = 2;
+            stored_left = l;
+        } else if (btype == 1) {
+            for (int i = 0; i < 288; ++i) lens[i] = i < 144 ? 8 : (i < 256 ? 9 : (i < 280 ? 7 : 8));
+            build(lit, lens, 288, false);
+            // all 32 fixed distance codes (30 and 31 never occur, RFC 1951 3.2.6)
+            for (int i = 0; i < 32; ++i) lens[i] = 5;
+            build(dist, lens, 32, false);
+        } else if (btype == 2) {
+            const int nlen = (int)b.get(5) + 257, ndist = (int)b.get(5) + 1, ncode = (int)b.get(4) + 4;
+            if (nlen > 286 || ndist > 30) return err = 3;
+            for (int i = 0; i < 19; ++i) lens[i] = 0;
+            for (int i = 0; i < ncode; ++i) lens[cl_order(i)] = (unsigned char)b.get(3);
+            if (!build(lit, lens, 19, true)) return err = 4;
+            int i = 0;
+            while (i < nlen + ndist) {
+                const int sym = decode(b, lit);
+                if (sym < 0 || b.over) return err = 5;
+                if (sym < 16) {
+                    lens[i++] = (unsigned char)sym;
+                    continue;
+                }
+                int rep = 0, val = 0;
+                if (sym == 16) {
+                    if (i == 0) return err = 6;
+                    val = lens[i - 1];
+                    rep = 3 + (int)b.get(2);
+                } else if (sym == 17) {
+                    rep = 3 + (int)b.get(3);
+                } else {
+                    rep = 11 + (int)b.get(7);
+                }
+                if (i + rep > nlen + ndist) return err = 7;
+                while (rep--) lens[i++] = (unsigned char)val;
+            }
+            if (lens[256] == 0) return err = 8;
+            if (!build(lit, lens, nlen, false)) return err = 9;
+            if (!build(dist, lens + nlen, ndist, false)) return err = 10;
+        } else {
+            return err = 11;
+        }
+        return 0;
+    }
+
     // Decodes until `cap` matches are recorded (batch[i] = {position,
     // length, distance}), the last block ends, or an error. Literals go to
     // dst directly; matches are for the caller to copy in order. Returns the
@@ -213,82 +268,7 @@ struct Inflater {
         while (!err && n < cap) {
             if (!in_block) {
                 if (final_block) break;
-                final_block = (int)b.get(1);
-                btype = (int)b.get(2);
-                in_block = 1;
-                if (btype == 0) {
-                    b.align();
-                    const unsigned l = b.get(16), nl = b.get(16);
-                    if ((l ^ 0xffffu) != nl || b.over) {
-                        err = 2;
-                        break;
-                    }
-                    stored_left = l;
-                } else if (btype == 1) {
-                    for (int i = 0; i < 288; ++i) lens[i] = i < 144 ? 8 : (i < 256 ? 9 : (i < 280 ? 7 : 8));
-                    build(lit, lens, 288, false);
-                    // all 32 fixed distance codes (30 and 31 never occur, RFC 1951 3.2.6)
-                    for (int i = 0; i < 32; ++i) lens[i] = 5;
-                    build(dist, lens, 32, false);
-                } else if (btype == 2) {
-                    const int nlen = (int)b.get(5) + 257, ndist = (int)b.get(5) + 1, ncode = (int)b.get(4) + 4;
-                    if (nlen > 286 || ndist > 30) {
-                        err = 3;
-                        break;
-                    }
-                    for (int i = 0; i < 19; ++i) lens[i] = 0;
-                    for (int i = 0; i < ncode; ++i) lens[cl_order(i)] = (unsigned char)b.get(3);
-                    if (!build(lit, lens, 19, true)) {
-                        err = 4;
-                        break;
-                    }
-                    int i = 0;
-                    while (i < nlen + ndist) {
-                        const int sym = decode(b, lit);
-                        if (sym < 0 || b.over) {
-                            err = 5;
-                            break;
-                        }
-                        if (sym < 16) {
-                            lens[i++] = (unsigned char)sym;
-                            continue;
-                        }
-                        int rep = 0, val = 0;
-                        if (sym == 16) {
-                            if (i == 0) {
-                                err = 6;
-                                break;
-                            }
-                            val = lens[i - 1];
-                            rep = 3 + (int)b.get(2);
-                        } else if (sym == 17) {
-                            rep = 3 + (int)b.get(3);
-                        } else {
-                            rep = 11 + (int)b.get(7);
-                        }
-                        if (i + rep > nlen + ndist) {
-                            err = 7;
-                            break;
-                        }
-                        while (rep--) lens[i++] = (unsigned char)val;
-                    }
-                    if (err) break;
-                    if (lens[256] == 0) {
-                        err = 8;
-                        break;
-                    }
-                    if (!build(lit, lens, nlen, false)) {
-                        err = 9;
-                        break;
-                    }
-                    if (!build(dist, lens + nlen, ndist, false)) {
-                        err = 10;
-                        break;
-                    }
-                } else {
-                    err = 11;
-                    break;
-                }
+                if (block_header(lit, dist, lens)) break;
             }
             if (btype == 0) {  // stored bytes (byte aligned)
                 while (stored_left > 0) {

@@ -33,3 +33,4 @@ extern "C" long long emu_inflate(const uint8_t *src, long long n, uint8_t *dst, 
     if (((b << 16) | a) != want) return -22;
     return z.op;
 }
+

@@ -67,3 +67,4 @@ def test_inflate_rejects_like_zlib(emu):
         assert inflate(emu, junk, 65536) == want
         agree += 1
     assert agree == 400
+
