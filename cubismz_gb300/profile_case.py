@@ -2,9 +2,11 @@
 larger than L2; 60 blobs, 6 interfaces, seed 3), compressed three times with
 wtype 1, threshold 1e-3 x range, zerobits 4, shuffle and the chosen lossless
 stage (LZ4 by default, or zlib), then decompressed twice. Prints the
-per-stage device times of each call.
+per-stage device times of each call. With --ingest, the same field goes
+through the HDF5 tools' layout instead: to z-fastest and back, three times
+each (the tile transpose kernels).
 
-    python -m cubismz_gb300.profile_case [--encoder lz4|zlib]
+    python -m cubismz_gb300.profile_case [--encoder lz4|zlib] [--ingest]
 """
 import argparse
 
@@ -14,7 +16,9 @@ import numpy as np
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--encoder", default="lz4", choices=["lz4", "zlib"])
-    enc = ap.parse_args().encoder
+    ap.add_argument("--ingest", action="store_true")
+    args = ap.parse_args()
+    enc = args.encoder
     import torch
     import cubismz_gb300 as cz
     from cubismz_gb300 import synth
@@ -22,6 +26,18 @@ def main():
     field = synth.generate(shape, seed=3, blobs=60, interfaces=6)
     eps = float(np.float32(1e-3 * (field.max() - field.min())))
     f = torch.from_numpy(field).cuda()
+    if args.ingest:
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        for _ in range(3):
+            ev[0].record()
+            z = cz.field_to_zfastest(f)
+            ev[1].record()
+            back = cz.field_from_zfastest(z)
+            ev[2].record()
+            torch.cuda.synchronize()
+            assert torch.equal(back, f)
+            print("to_zfastest ms", ev[0].elapsed_time(ev[1]), "from_zfastest ms", ev[1].elapsed_time(ev[2]))
+        return
     ctx = cz.context(0)
     ctx.set_timing(True)
     for _ in range(3):
