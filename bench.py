@@ -64,22 +64,85 @@ def peaks():
 
 
 class Clocks:
-    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    """Samples SM clocks and clock-event (throttle) reasons during the timed
+    region: NVML read queries through ctypes every millisecond, so that even
+    a timed region of a few milliseconds gets samples; nvidia-smi at its
+    20 ms interval where NVML cannot be loaded. Reads only."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
 
     def __init__(self, dev):
         self.dev = dev
         self.proc = None
+        self.nvml = None
         self.lines = []
+        self.samples = []  # (sm MHz, reasons bitmask) from NVML
+        self.max_mhz = 0.0
+        self.source = None
+
+    def _bus_id(self):
+        import torch
+        pr = torch.cuda.get_device_properties(self.dev)
+        if all(hasattr(pr, a) for a in ("pci_domain_id", "pci_bus_id", "pci_device_id")):
+            return f"{pr.pci_domain_id:08x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+        return None
+
+    def _open_nvml(self):
+        import ctypes as C
+        try:
+            L = C.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return False
+        if L.nvmlInit_v2() != 0:
+            return False
+        h = C.c_void_p()
+        bus = self._bus_id()
+        ok = bus is not None and L.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), C.byref(h)) == 0
+        if not ok and L.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.dev), C.byref(h)) != 0:
+            L.nvmlShutdown()
+            return False
+        mx = C.c_uint(0)
+        if L.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+        self.reason_fn = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            L.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.nvml, self.h = L, h
+        return True
+
+    def _poll(self):
+        import ctypes as C
+        clk, rs = C.c_uint(0), C.c_ulonglong(0)
+        while not self.stop:
+            if self.nvml.nvmlDeviceGetClockInfo(self.h, 1, C.byref(clk)) == 0:
+                r = rs.value if self.reason_fn(self.h, C.byref(rs)) == 0 else 0
+                self.samples.append((float(clk.value), r))
+            time.sleep(0.001)
 
     def __enter__(self):
+        self.stop = False
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+            have_nvml = self._open_nvml()
+        except (OSError, AttributeError):
+            have_nvml = False
+        if have_nvml:
+            self.source = "nvml"
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            t_end = time.time() + 1.0
+            while not self.samples and time.time() < t_end:
+                time.sleep(0.001)
+            self.samples.clear()  # samples from here on fall inside the timed region
+            return self
+        try:
+            target = self._bus_id() or str(self.dev)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", target, f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.source = "nvidia-smi"
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
             t_end = time.time() + 3.0  # sampling is live before the timed region starts
@@ -95,6 +158,10 @@ class Clocks:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self.stop = True
+        if self.nvml is not None:
+            self.t.join(timeout=2)
+            self.nvml.nvmlShutdown()
         if self.proc:
             self.proc.terminate()
             try:
@@ -103,8 +170,11 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], 0.0, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], self.max_mhz, set()
+        if self.source == "nvml":
+            for mhz, r in self.samples:
+                sm.append(mhz)
+                reasons.update(n for n, b in self.BITS.items() if r & b)
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
@@ -114,12 +184,14 @@ class Clocks:
                 mx = max(mx, float(parts[2]))
             except ValueError:
                 continue
-            for n, v in zip(names, parts[5:9]):
+            for n, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"],
+                            parts[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no clock samples"], "source": self.source}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "source": self.source}
 
 
 def make_field(seed):
@@ -141,6 +213,23 @@ def cpu_port_time(field, eps, threads, max_seconds=20.0):
         dt = min(dt, time.perf_counter() - t0)
         reps += 1
     return dt, f"full {SIZE}^3 field, best of {reps}"
+
+
+def cpu_thread_counts(field, eps, counts=(1, 12)):
+    """The CPU oracle port at fixed thread counts (1, and the 12 that the
+    reference's LZ4 branch allows, CompressionEncoders.h:197,209-212) on the
+    field's first 64 z-planes (512 blocks): GB/s per thread count, best of 2."""
+    from oracle import czoracle as O
+    slab = np.ascontiguousarray(field[:64])
+    out = {}
+    for t in counts:
+        best = float("inf")
+        for _ in range(2):
+            t0 = time.perf_counter()
+            O.field_compress(slab, eps, WTYPE, ZEROBITS, 1, 1, 1, t)
+            best = min(best, time.perf_counter() - t0)
+        out[str(t)] = slab.nbytes / best / 1e9
+    return out
 
 
 def batch_report(cz, dev, steps):
@@ -308,35 +397,37 @@ def run_stress(args):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     stream = torch.cuda.current_stream(dev)
     tot_c = tot_d = 0.0
-    for name, f in zip(names, fields):
-        rng_ = float(f.max() - f.min())
-        eps = float(np.float32(1e-3 * rng_))
-        cz.compress_field(f, eps, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")  # warm-up
-        ev[0].record(stream)
-        cf = cz.compress_field(f, eps, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
-        ev[1].record(stream)
-        data, off = cf.to_device()
-        ev[2].record(stream)
-        st = cz.diff_field(data, off, f.shape, f, WTYPE, SHUFFLE, encoder="lz4", file_bytes=cf.nbytes, out=dec)
-        ev[3].record(stream)
-        torch.cuda.synchronize()
-        c_ms, d_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
-        tot_c += c_ms
-        tot_d += d_ms
-        psnr = 20 * np.log10(rng_ / (2 * np.sqrt(st["e_2"] / st["n"])))
-        rf = cz.refit_field(f, eps, REFIT_ITERS, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
-        rd, ro = rf.to_device()
-        sr = cz.diff_field(rd, ro, f.shape, f, WTYPE, SHUFFLE, encoder="lz4", file_bytes=rf.nbytes, out=dec)
-        psnr_r = 20 * np.log10(rng_ / (2 * np.sqrt(sr["e_2"] / sr["n"])))
-        out["per_field"].append({"field": name, "compress_gbs": f.numel() * 4 / (c_ms * 1e-3) / 1e9,
-                                 "decompress_gbs": f.numel() * 4 / (d_ms * 1e-3) / 1e9,
-                                 "ratio": f.numel() * 4 / cf.nbytes, "psnr_db": psnr, "max_abs_err": st["e_inf"],
-                                 "res_line": st["res_line"],
-                                 "refit": {"ratio": f.numel() * 4 / rf.nbytes, "psnr_db": psnr_r,
-                                           "gain_db": psnr_r - psnr, "pre_lz4_bytes_equal": rf.raw_bytes == cf.raw_bytes}})
-        del data, off, rd, ro
+    with Clocks(0) as clk:  # spans the five fields (their timed calls and the untimed refits)
+        for name, f in zip(names, fields):
+            rng_ = float(f.max() - f.min())
+            eps = float(np.float32(1e-3 * rng_))
+            cz.compress_field(f, eps, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")  # warm-up
+            ev[0].record(stream)
+            cf = cz.compress_field(f, eps, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
+            ev[1].record(stream)
+            data, off = cf.to_device()
+            ev[2].record(stream)
+            st = cz.diff_field(data, off, f.shape, f, WTYPE, SHUFFLE, encoder="lz4", file_bytes=cf.nbytes, out=dec)
+            ev[3].record(stream)
+            torch.cuda.synchronize()
+            c_ms, d_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
+            tot_c += c_ms
+            tot_d += d_ms
+            psnr = 20 * np.log10(rng_ / (2 * np.sqrt(st["e_2"] / st["n"])))
+            rf = cz.refit_field(f, eps, REFIT_ITERS, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
+            rd, ro = rf.to_device()
+            sr = cz.diff_field(rd, ro, f.shape, f, WTYPE, SHUFFLE, encoder="lz4", file_bytes=rf.nbytes, out=dec)
+            psnr_r = 20 * np.log10(rng_ / (2 * np.sqrt(sr["e_2"] / sr["n"])))
+            out["per_field"].append({"field": name, "compress_gbs": f.numel() * 4 / (c_ms * 1e-3) / 1e9,
+                                     "decompress_gbs": f.numel() * 4 / (d_ms * 1e-3) / 1e9,
+                                     "ratio": f.numel() * 4 / cf.nbytes, "psnr_db": psnr, "max_abs_err": st["e_inf"],
+                                     "res_line": st["res_line"],
+                                     "refit": {"ratio": f.numel() * 4 / rf.nbytes, "psnr_db": psnr_r,
+                                               "gain_db": psnr_r - psnr, "pre_lz4_bytes_equal": rf.raw_bytes == cf.raw_bytes}})
+            del data, off, rd, ro
     out["compress_gbs"] = out["total_bytes"] / (tot_c * 1e-3) / 1e9
     out["decompress_gbs"] = out["total_bytes"] / (tot_d * 1e-3) / 1e9
+    out["clocks"] = clk.summary()
     print(json.dumps({"stress": out}), flush=True)
 
 
@@ -366,7 +457,9 @@ def run_reference(args, rank, world):
         "config": {"workload": f"compress {SIZE}^3 fp32 field, wtype 1, thr 1e-3*range, zerobits 4, shuffle, lz4",
                    "threads": threads},
         "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": kind,
-                         "sample": f"full {SIZE}^3 field per step"},
+                         "sample": f"full {SIZE}^3 field per step",
+                         "gbs_by_threads": cpu_thread_counts(field, eps),
+                         "by_threads_sample": f"first 64 z-planes of the {SIZE}^3 field (512 blocks)"},
         "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -520,7 +613,8 @@ def run_ours(args, rank, world, local_rank):
         "roofline": dominant,
         "roofline_kernels": [roof_enc, roof_lz],
         "cpu_baseline": {"value": nbytes / cpu_s / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "gbs_by_threads": cpu_thread_counts(field, eps),
+                         "by_threads_sample": f"first 64 z-planes of the {SIZE}^3 field (512 blocks)"},
         "zlib": zl,
         "refit": refit,
         "batched": batched,
