@@ -104,18 +104,18 @@ __device__ __forceinline__ void warp_copy(uint8_t *dst, const uint8_t *src, int 
     if (lane < t) dst[4 * nw + lane] = src[4 * nw + lane];
 }
 
-// n <= 32 bytes: all loads (16 bytes each, aligned words) issued before any
-// store (source and destination never overlap). May read up to 35 bytes
-// past s (inputs carry tail room).
+// n <= 32 bytes, 4 per step, so that the cost follows n (most literal runs
+// between matches are 0-4 bytes). Source and destination never overlap. May
+// read up to 7 bytes past s + n (inputs carry tail room).
 __device__ __forceinline__ void copy_short(uint8_t *__restrict__ d, const uint8_t *__restrict__ s, int n)
 {
-    if (n <= 0) return;
-    uint32_t v[8];
-    rd16u(s, *reinterpret_cast<uint32_t(*)[4]>(v));
-    if (n > 16) rd16u(s + 16, *reinterpret_cast<uint32_t(*)[4]>(v + 4));
-#pragma unroll
-    for (int i = 0; i < 32; ++i)
-        if (i < n) d[i] = (uint8_t)(v[i >> 2] >> (8 * (i & 3)));
+    for (int i = 0; i < n; i += 4) {
+        const uint32_t w = rd32u(s + i);
+        d[i] = (uint8_t)w;
+        if (i + 1 < n) d[i + 1] = (uint8_t)(w >> 8);
+        if (i + 2 < n) d[i + 2] = (uint8_t)(w >> 16);
+        if (i + 3 < n) d[i + 3] = (uint8_t)(w >> 24);
+    }
 }
 
 // Bytes of a length field's continuation: n/255 bytes of 255, then n%255.
@@ -170,11 +170,33 @@ constexpr int kSW = 512, kSub = kSW / 32, kMaxSeqLane = kSub / 4;
 constexpr uint32_t kPosMask = (1u << 18) - 1;
 __device__ __forceinline__ uint32_t lz_tag(uint32_t v) { return (v * 0x85ebca77u) >> 18; }
 
-// exact match length from (p, cand), starting `known` bytes in (lane-local);
-// 16 bytes per round trip to memory
+// 8 bytes at any byte address as two little-endian words (three aligned
+// loads). May read up to 11 bytes past p.
+__device__ __forceinline__ void rd8u(const uint8_t *p, uint32_t (&v)[2])
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+    const uint32_t sh = (uint32_t)(a & 3) * 8;
+    const uint32_t x0 = w[0], x1 = w[1], x2 = w[2];
+    v[0] = sh ? __funnelshift_r(x0, x1, sh) : x0;
+    v[1] = sh ? __funnelshift_r(x1, x2, sh) : x1;
+}
+
+// exact match length from (p, cand), starting `known` bytes in (lane-local):
+// the first 8 bytes on their own (most matches are 4-8 bytes long), then 16
+// bytes per round trip to memory
 __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, int known, int matchlimit)
 {
     int len = known;
+    {
+        uint32_t a[2], b[2];
+        rd8u(src + p + len, a);
+        rd8u(src + cand + len, b);
+        const uint32_t x0 = a[0] ^ b[0], x1 = a[1] ^ b[1];
+        const int k = x0 ? (__ffs(x0) - 1) >> 3 : x1 ? 4 + ((__ffs(x1) - 1) >> 3) : 8;
+        len += k;
+        if (k < 8) return len < matchlimit - p ? len : matchlimit - p;
+    }
     while (p + len < matchlimit) {
         uint32_t a[4], b[4];
         rd16u(src + p + len, a);

@@ -4,9 +4,10 @@ wtype 1, threshold 1e-3 x range, zerobits 4, shuffle and the chosen lossless
 stage (LZ4 by default, or zlib), then decompressed twice. Prints the
 per-stage device times of each call. With --ingest, the same field goes
 through the HDF5 tools' layout instead: to z-fastest and back, three times
-each (the tile transpose kernels).
+each (the tile transpose kernels). --shape nz,ny,nx picks another field
+size (multiples of 32), e.g. 512,512,512 for the bench's occupancy.
 
-    python -m cubismz_gb300.profile_case [--encoder lz4|zlib] [--ingest]
+    python -m cubismz_gb300.profile_case [--encoder lz4|zlib] [--ingest] [--shape nz,ny,nx]
 """
 import argparse
 
@@ -17,12 +18,13 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--encoder", default="lz4", choices=["lz4", "zlib"])
     ap.add_argument("--ingest", action="store_true")
+    ap.add_argument("--shape", default="256,512,512")
     args = ap.parse_args()
     enc = args.encoder
     import torch
     import cubismz_gb300 as cz
     from cubismz_gb300 import synth
-    shape = (256, 512, 512)
+    shape = tuple(int(x) for x in args.shape.split(","))
     field = synth.generate(shape, seed=3, blobs=60, interfaces=6)
     eps = float(np.float32(1e-3 * (field.max() - field.min())))
     f = torch.from_numpy(field).cuda()
