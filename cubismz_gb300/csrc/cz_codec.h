@@ -45,8 +45,7 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 // LZ4 stage (cz_lz4.cu). Chunk c's input is in[in_off[c] .. in_off[c]+in_len[c]);
 // the encoder reads it as aligned words, so in + in_off[c] must be a multiple
 // of 4 bytes (records and the staged host inputs are), and reads up to 64
-// bytes past its end (buffers carry tail room). Outputs may start anywhere;
-// a chunk's LZ4 output stays below 1 GiB.
+// bytes past its end (buffers carry tail room). Outputs may start anywhere.
 // records != 0: chunks hold block records with shuffled byte planes; the
 // search skips planes 1 and 2 (copied as literals).
 // warps: 2, 4, 8 or 32 warps (chunks) per CTA (32 fills an SM); any choice
