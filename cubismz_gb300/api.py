@@ -210,6 +210,36 @@ def compress_field(field, eps, wtype=1, zerobits=0, shuffle=False, encoder="lz4"
     return CompressedField(ctx, s, (nz, ny, nx), prm)
 
 
+def batch_compress(fields, eps, wtype=1, zerobits=0, shuffle=False, encoder="lz4", stream=None):
+    """cz_batch_compress: CUDA fields of uneven (nz, ny, nx) extents, one
+    threshold each, in one persistent wavelet launch over all their blocks
+    (one record per chunk). Returns a CompressedField per field; they share
+    the context's device buffers (valid until the next call on it)."""
+    import torch
+    for f in fields:
+        assert f.is_cuda and f.dtype == torch.float32 and f.is_contiguous()
+    n = len(fields)
+    dev = fields[0].device
+    ctx = context(dev.index or 0)
+    ptrs = (C.c_void_p * n)(*[f.data_ptr() for f in fields])
+    dims = (C.c_int * (3 * n))(*[d for f in fields for d in (f.shape[2], f.shape[1], f.shape[0])])
+    e = (C.c_float * n)(*[float(x) for x in eps])
+    prm = params(0.0, wtype, zerobits, shuffle, encoder, 1)
+    outs = (Stream * n)()
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    ctx.check(ctx.L.cz_batch_compress(ctx.h, n, ptrs, dims, e, C.byref(prm), C.c_void_p(st), outs))
+    res = []
+    for i, f in enumerate(fields):
+        s = Stream(outs[i].data, outs[i].data_bytes, outs[i].chunk_offsets, outs[i].nchunks, outs[i].nblocks,
+                   outs[i].raw_bytes)
+        # a field's size is its last rebased chunk offset
+        off = torch.empty(s.nchunks + 1, dtype=torch.int64, device=dev)
+        ctx.check(ctx.L.cz_stream_copy(ctx.h, C.byref(s), None, C.c_void_p(off.data_ptr()), C.c_void_p(st)))
+        s.data_bytes = int(off[-1].item())
+        res.append(CompressedField(ctx, s, tuple(f.shape), prm))
+    return res
+
+
 class Plan:
     """A batch of CUDA fields (shape (nz, ny, nx), float32, contiguous) with
     per-field thresholds, compressed by one captured CUDA graph (one
