@@ -23,6 +23,13 @@ Outputs (in this directory):
                        small synthetic field and of their LZ4_compress output.
   ref_lz4_chunks.bin small LZ4 streams produced by the reference LZ4_compress
                      (length-prefixed), for the GPU decoder tests.
+  lz4_cases.json     the reference LZ4_uncompress_unknownOutputSize
+                     (lz4.c:802-905) on seeded inputs: random bytes, valid
+                     reference streams at exact, short and generous output
+                     capacities, and the same streams with bytes changed or
+                     cut; per case its return value (output size, or minus
+                     the input position of the error) and the output's
+                     sha256. Regenerate alone with --lz4-cases.
 """
 import hashlib
 import io
@@ -86,9 +93,57 @@ def sha(b):
     return hashlib.sha256(bytes(b)).hexdigest()
 
 
+def lz4_cases():
+    """Seeded LZ4 decoder cases, decoded by the reference's own decoder."""
+    L = O.ref(4, 1, "lz4")
+    rng = np.random.default_rng(77)
+    small = synth.config_field("small", 0)
+    raw, off = O.field_compress(small, 1e-2, 1, 4, 1, 0, 1)
+    plain = [raw[off[3]:off[3] + 2000].tobytes(), bytes(3000), b"abc" * 700,
+             rng.integers(0, 256, 500, np.uint8).tobytes(),
+             b"".join(bytes(rng.integers(0, 256, int(rng.integers(1, 40)), np.uint8)) + bytes([int(rng.integers(0, 256))])
+                      * int(rng.integers(4, 90)) for _ in range(30))]
+    streams = [O.ref_lz4_compress(L, d).tobytes() for d in plain]
+    cases = []
+
+    def add(kind, data, cap, base=None, edits=None, cut=None):
+        n, out = O.ref_lz4_decompress(L, data, cap)
+        c = {"kind": kind, "cap": cap, "ref": int(n), "sha": sha(out.tobytes()) if n > 0 else ""}
+        if base is None:
+            c["hex"] = data.hex()
+        else:
+            c["base"] = base
+            if edits:
+                c["edits"] = edits
+            if cut is not None:
+                c["cut"] = cut
+        cases.append(c)
+
+    for i in range(60):
+        add("junk", rng.integers(0, 256, int(rng.integers(1, 300)), np.uint8).tobytes(), 4096 if i % 2 else 64)
+    for b, (z, d) in enumerate(zip(streams, plain)):
+        for cap in (len(d), len(d) - 1, len(d) // 2, len(d) + 100):
+            add("valid", z, cap, base=b)
+        for _ in range(12):
+            edits = [[int(rng.integers(0, len(z))), int(rng.integers(0, 256))] for _ in range(int(rng.integers(1, 3)))]
+            m = bytearray(z)
+            for pos, val in edits:
+                m[pos] = val
+            add("edited", bytes(m), len(d), base=b, edits=edits)
+        for cut in sorted(set(int(x) for x in rng.integers(1, len(z), 6))):
+            add("cut", z[:cut], len(d), base=b, cut=cut)
+    return {"streams": [z.hex() for z in streams], "cases": cases}
+
+
 def main():
     if not os.path.isdir(REF):
         sys.exit("reference tree not found")
+    if sys.argv[1:] == ["--lz4-cases"]:
+        with open(os.path.join(HERE, "lz4_cases.json"), "w") as f:
+            json.dump(lz4_cases(), f)
+        return
+    with open(os.path.join(HERE, "lz4_cases.json"), "w") as f:
+        json.dump(lz4_cases(), f)
     field = demo_field()
     with open(os.path.join(HERE, "demo128_f32.xz"), "wb") as f:
         f.write(lzma.compress(field.tobytes(), preset=9))

@@ -168,3 +168,27 @@ def parse_cz(img):
         base += agg
     assert base == hoff
     return {"blocks": dims, "subdomain": sub, "meta": meta, "ranks": ranks, "keys": keys}
+
+
+def lz4_cases():
+    """The reference LZ4 decoder's results on seeded inputs
+    (tests/golden/lz4_cases.json, made by tests/golden/make_golden.py):
+    yields (input bytes, output capacity, reference return value, sha256 of
+    the reference's output or "")."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "lz4_cases.json")) as f:
+        d = json.load(f)
+    streams = [bytes.fromhex(h) for h in d["streams"]]
+    for c in d["cases"]:
+        if "hex" in c:
+            data = bytes.fromhex(c["hex"])
+        else:
+            data = bytearray(streams[c["base"]])
+            for pos, val in c.get("edits", []):
+                data[pos] = val
+            if "cut" in c:
+                data = data[: c["cut"]]
+            data = bytes(data)
+        yield data, c["cap"], c["ref"], c["sha"]
+

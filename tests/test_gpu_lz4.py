@@ -94,3 +94,25 @@ def test_gpu_lz4_decodes_constructed_streams(cz):
             assert n <= 0
             with pytest.raises(cz.CzError):
                 cz.lz4_decompress(z, cap)
+
+
+def test_gpu_lz4_returns_the_reference_decoder_results(cz):
+    """Through the C ABI, cz_lz4_decompress writes what the reference's
+    LZ4_uncompress_unknownOutputSize returned on the same input and
+    capacity -- the output size, or minus the input position of the error --
+    and the same output bytes."""
+    import ctypes as C
+    import hashlib
+    from tests.helpers import lz4_cases
+    ctx = cz.context(0)
+    for data, cap, ref, ref_sha in lz4_cases():
+        src = np.frombuffer(data, np.uint8).copy()
+        dst = np.zeros(max(cap, 1), np.uint8)
+        n = C.c_int(0)
+        rc = ctx.L.cz_lz4_decompress(ctx.h, src.ctypes.data_as(C.POINTER(C.c_uint8)), src.size,
+                                     dst.ctypes.data_as(C.POINTER(C.c_uint8)), cap, C.byref(n))
+        assert n.value == ref, (len(data), cap, n.value, ref)
+        assert (rc == 0) == (ref >= 0)
+        if ref > 0:
+            assert hashlib.sha256(dst[:ref].tobytes()).hexdigest() == ref_sha
+

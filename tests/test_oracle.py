@@ -65,6 +65,22 @@ def test_oracle_lz4_roundtrip_and_errors():
     assert n <= 0
 
 
+def test_oracle_lz4_decoder_matches_reference_cases():
+    """The restated LZ4_uncompress_unknownOutputSize returns what the
+    reference's own decoder returned (output size, or minus the input
+    position of the error) on random, valid, edited and cut inputs, and the
+    same output bytes."""
+    from tests.helpers import lz4_cases
+    seen = 0
+    for data, cap, ref, ref_sha in lz4_cases():
+        n, out = O.lz4_decompress(data, cap)
+        assert n == ref, (len(data), cap, n, ref)
+        if ref > 0:
+            assert sha(out) == ref_sha
+        seen += 1
+    assert seen > 150
+
+
 ref_missing = O.ref(0, 0, "none") is None
 
 
