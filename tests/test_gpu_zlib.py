@@ -64,6 +64,33 @@ def test_inflate_rejects_malformed(cz):
             assert cz.zlib_decompress(junk, 65536) == want
 
 
+def test_inflate_edited_streams_like_zlib(cz):
+    """Valid streams (dynamic, fixed and stored blocks) with one byte
+    changed: the GPU inflate fails where zlib fails and otherwise returns
+    zlib's bytes."""
+    rng = np.random.default_rng(11)
+    d = (rng.integers(0, 6, 20000, np.uint8).tobytes() + bytes(3000) + b"pattern-" * 400
+         + rng.integers(0, 256, 2000, np.uint8).tobytes())
+    streams = [zlib.compress(d, 6), zlib.compress(d, 1), zlib.compress(d, 0)]
+    co = zlib.compressobj(9, zlib.DEFLATED, 15, 9, zlib.Z_FIXED)
+    streams.append(co.compress(d) + co.flush())
+    for z in streams:
+        for _ in range(25):
+            e = bytearray(z)
+            pos = int(rng.integers(0, len(z)))
+            e[pos] = (e[pos] + int(rng.integers(1, 256))) & 255
+            e = bytes(e)
+            try:
+                want = zlib.decompress(e)
+            except zlib.error:
+                want = None
+            if want is None or len(want) > len(d):
+                with pytest.raises(cz.CzError):
+                    cz.zlib_decompress(e, len(d))
+            else:
+                assert cz.zlib_decompress(e, len(d)) == want
+
+
 def test_published_golden_zlib_file_on_gpu(cz, golden, demo_field):
     from cubismz_gb300 import api, shard
     raw, off = O.field_compress(demo_field, 5e-5, 3, 0, 0, 0, 1)

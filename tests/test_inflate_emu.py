@@ -68,3 +68,31 @@ def test_inflate_rejects_like_zlib(emu):
         agree += 1
     assert agree == 400
 
+
+def edited_streams(seed=11, per=25):
+    """Valid streams (dynamic, fixed and stored blocks) with one byte
+    changed, seeded."""
+    rng = np.random.default_rng(seed)
+    d = (rng.integers(0, 6, 20000, np.uint8).tobytes() + bytes(3000) + b"pattern-" * 400
+         + rng.integers(0, 256, 2000, np.uint8).tobytes())
+    streams = [zlib.compress(d, 6), zlib.compress(d, 1), zlib.compress(d, 0)]
+    co = zlib.compressobj(9, zlib.DEFLATED, 15, 9, zlib.Z_FIXED)
+    streams.append(co.compress(d) + co.flush())
+    for z in streams:
+        for _ in range(per):
+            e = bytearray(z)
+            pos = int(rng.integers(0, len(z)))
+            e[pos] = (e[pos] + int(rng.integers(1, 256))) & 255
+            yield bytes(e), len(d)
+
+
+def test_inflate_edited_streams_like_zlib(emu):
+    for e, cap in edited_streams(per=60):
+        try:
+            want = zlib.decompress(e)
+        except zlib.error:
+            want = None
+        if want is not None and len(want) > cap:
+            want = None
+        assert inflate(emu, e, cap) == want
+
