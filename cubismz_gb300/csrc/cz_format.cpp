@@ -200,6 +200,17 @@ int parse_image(const uint8_t *img, long long size, Parsed &out, std::string &er
         err = "missing block counts";
         return -1;
     }
+    // every block takes 20 bytes of metadata, which bounds the products
+    // below before they are formed; a subdomain is no larger than the grid
+    const long long room = (size - pos) / 20;
+    if (out.bx > room || out.by > room / out.bx || out.bz > room / ((long long)out.bx * out.by)) {
+        err = "truncated block metadata";
+        return -1;
+    }
+    if (sub[0] > out.bx || sub[1] > out.by || sub[2] > out.bz) {
+        err = "SubdomainBlocks larger than Blocks";
+        return -1;
+    }
     const long long nblocks = (long long)out.bx * out.by * out.bz;
     const long long bps = (long long)sub[0] * sub[1] * sub[2];
     if (nblocks % bps) {
@@ -207,10 +218,6 @@ int parse_image(const uint8_t *img, long long size, Parsed &out, std::string &er
         return -1;
     }
     const long long nsub = nblocks / bps;
-    if (pos + 20 * nblocks > size) {
-        err = "truncated block metadata";
-        return -1;
-    }
     std::vector<int> meta(5 * nblocks);
     memcpy(meta.data(), img + pos, (size_t)(20 * nblocks));
     pos += 20 * nblocks;
@@ -228,27 +235,31 @@ int parse_image(const uint8_t *img, long long size, Parsed &out, std::string &er
     out.chunk_size.clear();
     long long base = mini;
     std::vector<long long> first_chunk(nsub);
+    std::vector<int> sub_chunks(nsub);
     for (long long s = 0; s < nsub; ++s) {
         unsigned long long agg;
         int nch;
         memcpy(&agg, img + pos + 12 * s, 8);
         memcpy(&nch, img + pos + 12 * s + 8, 4);
-        if (nch <= 0 || (long long)agg < 8LL * nch || base + (long long)agg > (long long)hoff) {
+        // agg bytes of this subdomain lie between base and the header, and
+        // end in its LUT of nch offsets (compared without forming base + agg)
+        if (nch <= 0 || agg > (unsigned long long)(hoff - base) || agg < 8ULL * (unsigned long long)nch) {
             err = "bad HeaderLUT";
             return -1;
         }
         first_chunk[s] = (long long)out.chunk_start.size();
-        const long long lutstart = base + (long long)agg - 8LL * nch;
+        sub_chunks[s] = nch;
+        const unsigned long long data = agg - 8ULL * (unsigned long long)nch;  // chunk bytes before the LUT
         std::vector<unsigned long long> lut(nch);
-        memcpy(lut.data(), img + lutstart, 8 * (size_t)nch);
+        memcpy(lut.data(), img + base + (long long)data, 8 * (size_t)nch);
         for (int i = 0; i < nch; ++i) {
-            const long long end = (i + 1 < nch) ? (long long)lut[i + 1] : (long long)agg - 8LL * nch;
-            if ((long long)lut[i] >= end) {
-                err = "non-increasing chunk LUT";
+            const unsigned long long end = (i + 1 < nch) ? lut[i + 1] : data;
+            if (lut[i] >= end || end > data) {
+                err = "chunk LUT not increasing within the subdomain";
                 return -1;
             }
             out.chunk_start.push_back(base + (long long)lut[i]);
-            out.chunk_size.push_back(end - (long long)lut[i]);
+            out.chunk_size.push_back((long long)(end - lut[i]));
         }
         base += (long long)agg;
     }
@@ -269,7 +280,7 @@ int parse_image(const uint8_t *img, long long size, Parsed &out, std::string &er
             return -1;
         }
         const long long gc = first_chunk[s] + m[0];
-        if (gc >= (long long)out.chunk_start.size()) {
+        if (m[0] >= sub_chunks[s]) {
             err = "block metadata names a missing chunk";
             return -1;
         }
