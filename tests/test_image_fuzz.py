@@ -70,8 +70,7 @@ def _sub(img, key, value):
     """The image with the ASCII header line `key: ...` replaced."""
     pat = re.compile(rb"\n" + key.encode() + rb":[^\n]*\n")
     assert pat.search(img)
-    head, tail = img[:8], img[8:]
-    hoff = int(np.frombuffer(head, np.uint64)[0])
+    hoff = int(np.frombuffer(img[:8], np.uint64)[0])
     new = pat.sub(b"\n" + key.encode() + b": " + value.encode() + b"\n", img[hoff:], count=1)
     return img[:hoff] + new
 
@@ -113,3 +112,28 @@ def test_out_of_range_chunk_offsets_are_rejected(lib, image, k, value):
     b[lut0 + 8 * i:lut0 + 8 * i + 8] = np.uint64(value).tobytes()
     rc, _, _ = info(lib, b)
     assert rc in (CZ_E_ARG, CZ_E_CORRUPT)
+
+
+@pytest.mark.gpu
+def test_damaged_chunks_decode_or_fail_cleanly(gpu_lib, image, small_field):
+    """cz_decompress_image on images with changed chunk bytes: each decodes
+    or raises CzError, and afterwards the intact image still decodes to the
+    same field (the context stays usable)."""
+    import cubismz_gb300 as cz
+    img, n = image
+    good = cz.decompress_image(img, 1, True)
+    hoff = int(np.frombuffer(img[:8], np.uint64)[0])
+    mini = 8 + len(b"\n==============START-BINARY-OCEAN==============\n")
+    rng = np.random.default_rng(9)
+    failed = 0
+    for _ in range(60):
+        b = bytearray(img)
+        for _ in range(int(rng.integers(1, 4))):
+            b[int(rng.integers(mini, hoff - 8 * n))] = int(rng.integers(0, 256))
+        try:
+            cz.decompress_image(bytes(b), 1, True)
+        except cz.CzError:
+            failed += 1
+    assert failed > 0
+    assert np.array_equal(cz.decompress_image(img, 1, True).view(np.uint32), good.view(np.uint32))
+
