@@ -147,7 +147,11 @@ int cz_field_compress(cz_ctx *ctx, const float *d_field, int nx, int ny, int nz,
 int cz_stream_copy(cz_ctx *ctx, const cz_stream *s, uint8_t *d_data, long long *d_chunk_offsets, void *stream);
 /* Decompress chunks (d_data, d_chunk_offsets[nchunks+1], device) holding
  * the records of the field's blocks in block order, blocks_per_chunk per
- * chunk, into d_field. */
+ * chunk, into d_field. The offsets must lie within d_data's buffer (as the
+ * ones cz_stream_copy writes do; files go through the parser of
+ * cz_decompress_image, which checks them); a chunk whose end precedes its
+ * start, malformed chunks and malformed records are reported as
+ * CZ_E_CORRUPT. */
 int cz_field_decompress(cz_ctx *ctx, const uint8_t *d_data, const long long *d_chunk_offsets, int nchunks, int nx,
                         int ny, int nz, const cz_params *p, void *stream, float *d_field);
 
