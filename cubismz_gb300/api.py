@@ -9,13 +9,14 @@ device memory and streams only. Errors raise CzError, as the reference
 aborts.
 """
 import ctypes as C
+import threading
 
 import numpy as np
 
 from . import _lib
 from ._lib import CzError, Params, Stream
 
-_CTX = {}
+_TLS = threading.local()  # contexts per host thread: a context's calls must not overlap
 
 
 class Context:
@@ -56,10 +57,14 @@ class Context:
 
 
 def context(device=0):
-    """Process-wide context per device."""
-    if device not in _CTX:
-        _CTX[device] = Context(device)
-    return _CTX[device]
+    """This host thread's context on `device` (each thread has its own, as
+    each OpenMP thread of the reference has its own compressor)."""
+    ctxs = getattr(_TLS, "ctxs", None)
+    if ctxs is None:
+        ctxs = _TLS.ctxs = {}
+    if device not in ctxs:
+        ctxs[device] = Context(device)
+    return ctxs[device]
 
 
 def params(eps, wtype=1, zerobits=0, shuffle=False, encoder="none", blocks_per_chunk=1):

@@ -196,20 +196,19 @@ using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// Looked up once; the initialisation of a function-local static is
+// thread-safe, so contexts on several host threads may reach it together.
 EncodeTiled encode_tiled()
 {
-    static EncodeTiled fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const EncodeTiled fn = []() -> EncodeTiled {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiled>(p);
+        const bool ok = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                                         &q) == cudaSuccess &&
+                        q == cudaDriverEntryPointSuccess;
         cudaGetLastError();
-    }
+        return ok ? reinterpret_cast<EncodeTiled>(p) : nullptr;
+    }();
     return fn;
 }
 

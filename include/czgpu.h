@@ -80,7 +80,10 @@ typedef struct {
 
 /* ---- context ---------------------------------------------------------- */
 /* New context on `device` (scratch buffers are allocated on first use and
- * grown as needed). */
+ * grown as needed). Calls on one context must not overlap: use one context
+ * per host thread, as the reference uses one compressor object per OpenMP
+ * thread; contexts are independent of each other. A cz_stream points into
+ * its context's buffers and stays valid until the next call on it. */
 int cz_create(int device, cz_ctx **out);
 int cz_destroy(cz_ctx *ctx);
 /* Last error text of the context (never NULL). */

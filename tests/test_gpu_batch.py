@@ -94,3 +94,39 @@ def test_batch_compress_equals_single_fields(cz, encoder):
         ref = O.field_decompress(*O.field_compress(f, e, 1, 4, 1), f.shape, 1, 1)
         assert np.array_equal(dec, ref)
 
+
+def test_threads_compress_concurrently(cz):
+    """Host threads compress at the same time, each through its own
+    context, and get the bytes a single thread gets."""
+    import threading
+    import torch
+    from cubismz_gb300 import synth
+    shapes = [(64, 64, 96), (32, 96, 64), (96, 32, 32), (64, 32, 64)]
+    fields = [torch.from_numpy(synth.generate(s, seed=40 + i, blobs=6, interfaces=2)).cuda()
+              for i, s in enumerate(shapes)]
+    eps = [float(np.float32(1e-3 * float(f.max() - f.min()))) for f in fields]
+    want = [cz.compress_field(f, e, 1, 4, True, encoder="lz4").to_device() for f, e in zip(fields, eps)]
+    want = [(d.cpu(), o.cpu()) for d, o in want]
+    got, errors = [None] * len(fields), []
+
+    def work(i):
+        try:
+            torch.cuda.set_device(0)
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for _ in range(3):
+                    d, o = cz.compress_field(fields[i], eps[i], 1, 4, True, encoder="lz4", stream=s).to_device(s)
+                s.synchronize()
+            got[i] = (d.cpu(), o.cpu())
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(len(fields))]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors
+    for (wd, wo), (gd, go) in zip(want, got):
+        assert torch.equal(wd, gd) and torch.equal(wo, go)
+
