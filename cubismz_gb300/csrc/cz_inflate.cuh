@@ -186,9 +186,12 @@ CZ_HD int decode(Bits &b, const Huff &h)
 // Decoder state across batches.
 struct Inflater {
     Bits b;
-    long long op;  // output written so far (literals and recorded matches)
+    long long op;  // output written so far (literals, recorded matches and runs)
     int err, final_block, in_block, btype;
     long long stored_left;
+    // a stored block's bytes, for the caller to copy: input position,
+    // output position, length (run_n = 0: none)
+    long long run_src, run_dst, run_n;
 
     // Reads the zlib header; err != 0 if it is not a deflate stream without
     // a preset dictionary (RFC 1950 2.2).
@@ -198,6 +201,7 @@ struct Inflater {
         op = 0;
         err = final_block = in_block = btype = 0;
         stored_left = 0;
+        run_src = run_dst = run_n = 0;
         const unsigned cmf = b.get(8), flg = b.get(8);
         if ((cmf & 15) != 8 || (cmf >> 4) > 7 || ((cmf << 8) | flg) % 31 || (flg & 32)) err = 1;
     }
@@ -258,34 +262,41 @@ struct Inflater {
     }
 
     // Decodes until `cap` matches are recorded (batch[i] = {position,
-    // length, distance}), the last block ends, or an error. Literals go to
-    // dst directly; matches are for the caller to copy in order. Returns the
-    // number of matches recorded.
+    // length, distance}), a stored block's bytes are reached, the last block
+    // ends, or an error. Literals go to dst directly; matches are for the
+    // caller to copy in order, and so is a stored block (run_src, run_dst,
+    // run_n: input to output, disjoint from the matches). Returns the number
+    // of matches recorded.
     CZ_MEM int step(uint8_t *dst, long long oend, int (*batch)[3], int cap, Huff &lit, Huff &dist,
                    unsigned char *lens)
     {
         int n = 0;
+        run_n = 0;
         while (!err && n < cap) {
             if (!in_block) {
                 if (final_block) break;
                 if (block_header(lit, dist, lens)) break;
             }
-            if (btype == 0) {  // stored bytes (byte aligned)
-                while (stored_left > 0) {
-                    if (op >= oend) {
-                        err = 12;
-                        break;
-                    }
-                    const unsigned v = b.get(8);
-                    if (b.over) {
-                        err = 13;
-                        break;
-                    }
-                    dst[op++] = (uint8_t)v;
-                    --stored_left;
+            if (btype == 0) {  // stored bytes (byte aligned): one run for the caller
+                const long long from = b.pos - b.cnt / 8;  // next unread input byte (cnt is whole bytes here)
+                if (op + stored_left > oend) {
+                    err = 12;
+                    break;
                 }
+                if (from + stored_left > b.end) {
+                    err = 13;
+                    break;
+                }
+                run_src = from;
+                run_dst = op;
+                run_n = stored_left;
+                op += stored_left;
+                b.pos = from + stored_left;
+                b.buf = 0;
+                b.cnt = 0;
+                stored_left = 0;
                 in_block = 0;
-                continue;
+                break;  // copied before the next step
             }
             // literals while at least 8 input and 8 output bytes remain: one
             // table lookup each and no per-symbol end tests (a refill then

@@ -35,6 +35,25 @@ using namespace zl;
 
 constexpr int kZBatch = 128;  // matches per batch
 
+// n bytes from s to d by the warp (4-byte stores once d is aligned); every
+// load is of an aligned word holding at least one byte of the run.
+__device__ __forceinline__ void run_copy(uint8_t *d, const uint8_t *s, int n, int lane)
+{
+    int h = (int)((4 - (reinterpret_cast<uintptr_t>(d) & 3)) & 3);
+    if (h > n) h = n;
+    if (lane < h) d[lane] = s[lane];
+    d += h;
+    s += h;
+    n -= h;
+    const int nw = n >> 2;
+    const uint32_t sa = (uint32_t)(reinterpret_cast<uintptr_t>(s) & 3);
+    const uint32_t *sw = reinterpret_cast<const uint32_t *>(s - sa);
+    uint32_t *dw = reinterpret_cast<uint32_t *>(d);
+    for (int i = lane; i < nw; i += 32) dw[i] = sa ? __funnelshift_r(sw[i], sw[i + 1], 8 * sa) : sw[i];
+    const int t = n & 3;
+    if (lane < t) d[4 * nw + lane] = s[4 * nw + lane];
+}
+
 __global__ void __launch_bounds__(32)
 inflate_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
                uint8_t *__restrict__ out, const long long *out_off, const int *out_cap, int *out_len)
@@ -44,6 +63,7 @@ inflate_kernel(const uint8_t *__restrict__ in, const long long *in_off, const in
     __shared__ int batch[kZBatch][3];  // matches: output position, length, distance
     __shared__ int mpre[kZBatch + 1];  // exclusive prefix of the match lengths
     __shared__ int s_state[4];         // matches in the batch, error, done, Adler-32 of the trailer
+    __shared__ long long s_run[3];     // a stored block: input position, output position, length
     const int lane = threadIdx.x;
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint8_t *src = in + in_off[c];
@@ -56,8 +76,12 @@ inflate_kernel(const uint8_t *__restrict__ in, const long long *in_off, const in
                 s_state[0] = z.step(dst, oend, batch, kZBatch, lit, dist, lens);
                 s_state[1] = z.err;
                 s_state[2] = z.done();
+                s_run[0] = z.run_src;
+                s_run[1] = z.run_dst;
+                s_run[2] = z.err ? 0 : z.run_n;
             }
             __syncwarp();
+            if (s_run[2] > 0) run_copy(dst + s_run[1], src + s_run[0], (int)s_run[2], lane);
             // the batch's match bytes, all in parallel: byte k of a match at p
             // with distance d is out[p - d + (k mod d)]; where that lies in an
             // earlier match of the batch (or this one) the source is followed

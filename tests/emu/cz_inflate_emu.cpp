@@ -15,6 +15,7 @@ extern "C" long long emu_inflate(const uint8_t *src, long long n, uint8_t *dst, 
     z.start(src, n);
     for (;;) {
         const int m = z.step(dst, cap, batch, 128, lit, dist, lens);
+        if (!z.err && z.run_n > 0) memcpy(dst + z.run_dst, src + z.run_src, (size_t)z.run_n);
         for (int i = 0; i < m; ++i)
             for (int k = 0; k < batch[i][1]; ++k) {
                 const int p = batch[i][0], d = batch[i][2];
