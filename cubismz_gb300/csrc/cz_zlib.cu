@@ -278,9 +278,9 @@ struct Ring {
         flushed = to;
         __syncwarp();
     }
-    __device__ void make_room(int lane)
+    __device__ void make_room(int lane, int words = 52)
     {
-        if ((bp >> 5) + 52 >= flushed + kRingW) flush_to(bp >> 5, lane);
+        if ((bp >> 5) + words >= flushed + kRingW) flush_to(bp >> 5, lane);
     }
 };
 
@@ -349,45 +349,57 @@ __device__ int block_items(DeflateWarp &s, const unsigned long long *seq, int ns
         s.k0[lane] = k0;
         const int total = __shfl_sync(0xffffffffu, ii, 31);
         __syncwarp();
-        for (int t0 = 0; t0 < total; t0 += 32) {
-            if (MODE == 1) rg->make_room(lane);
-            const int t = t0 + lane;
-            int byte = 256 + lane, nb = 0;  // inactive lanes never group
-            unsigned long long v = 0;
-            if (t < total) {
-                const int j = find_item(s.end, t);
-                const int k = t - s.beg[j];
-                if (k < s.nlit[j]) {
-                    byte = src[s.litpos[j] + k];
-                    if (MODE == 1) {
-                        v = s.codes.lcode[byte];
-                        nb = s.codes.llen[byte];
-                    }
-                } else {
-                    const int mj = s.mlen[j], pk = s.k0[j] + k - s.nlit[j];
-                    const int pl = zl::piece_len(mj, pk);
-                    if (MODE == 0) {
-                        atomicAdd(&s.lf[257 + zl::len_sym(pl)], 1u);
-                        atomicAdd(&s.df[zl::dist_sym(s.dist[j])], 1u);
-                    } else {
-                        nb = zl::match_bits(s.codes, pl, s.dist[j], v);
-                    }
-                }
-            }
-            if (MODE == 0) {
-                const unsigned grp = __match_any_sync(0xffffffffu, byte);
-                if (byte < 256 && lane == __ffs(grp) - 1) atomicAdd(&s.lf[byte], (unsigned)__popc(grp));
-            } else {
-                int bi = nb;
+        // kU steps of 32 items at a time: their literal bytes are loaded
+        // together, then the steps are counted or written in order
+        constexpr int kU = 4;
+        for (int t0 = 0; t0 < total; t0 += 32 * kU) {
+            if (MODE == 1) rg->make_room(lane, 48 * kU + 4);
+            int byte[kU], nb[kU];  // byte >= 256: not a literal (inactive lanes never group)
+            unsigned long long v[kU];
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int u = __shfl_up_sync(0xffffffffu, bi, o);
-                    if (lane >= o) bi += u;
+            for (int u = 0; u < kU; ++u) {
+                const int t = t0 + 32 * u + lane;
+                byte[u] = 256 + lane;
+                nb[u] = 0;
+                v[u] = 0;
+                if (t < total) {
+                    const int j = find_item(s.end, t);
+                    const int k = t - s.beg[j];
+                    if (k < s.nlit[j]) {
+                        byte[u] = src[s.litpos[j] + k];
+                    } else {
+                        const int mj = s.mlen[j], pk = s.k0[j] + k - s.nlit[j];
+                        const int pl = zl::piece_len(mj, pk);
+                        if (MODE == 0) {
+                            atomicAdd(&s.lf[257 + zl::len_sym(pl)], 1u);
+                            atomicAdd(&s.df[zl::dist_sym(s.dist[j])], 1u);
+                        } else {
+                            nb[u] = zl::match_bits(s.codes, pl, s.dist[j], v[u]);
+                        }
+                    }
                 }
-                if (nb) ring_or(rg->ring, rg->bp + bi - nb, v);
-                rg->bp += __shfl_sync(0xffffffffu, bi, 31);
-                __syncwarp();  // the next step's flush reads these words
             }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                if (MODE == 0) {
+                    const unsigned grp = __match_any_sync(0xffffffffu, byte[u]);
+                    if (byte[u] < 256 && lane == __ffs(grp) - 1) atomicAdd(&s.lf[byte[u]], (unsigned)__popc(grp));
+                } else {
+                    if (byte[u] < 256) {
+                        v[u] = s.codes.lcode[byte[u]];
+                        nb[u] = s.codes.llen[byte[u]];
+                    }
+                    int bi = nb[u];
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int w = __shfl_up_sync(0xffffffffu, bi, o);
+                        if (lane >= o) bi += w;
+                    }
+                    if (nb[u]) ring_or(rg->ring, rg->bp + bi - nb[u], v[u]);
+                    rg->bp += __shfl_sync(0xffffffffu, bi, 31);
+                }
+            }
+            if (MODE == 1) __syncwarp();  // the next flush reads these words
         }
         __syncwarp();
         const bool last = pos + span_total >= hi || i0 + 32 >= nseq;
