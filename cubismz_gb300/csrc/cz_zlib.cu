@@ -238,6 +238,36 @@ __device__ bool warp_code(DeflateWarp &s, const uint32_t *freq, int n, uint8_t *
     return ok != 0;
 }
 
+// zl::data_bits (with the dynamic lengths) and zl::fixed_block_bits of the
+// block's counts, summed by the warp instead of lane 0; the same integers.
+__device__ void warp_block_bits(const DeflateWarp &s, const uint8_t *llen, const uint8_t *dlen, int lane,
+                                long long &data, long long &fixed)
+{
+    long long a = 0, f = 0;
+    for (int x = lane; x < zl::kLitSyms; x += 32) {
+        const long long c = s.lf[x];
+        a += c * llen[x];
+        f += c * zl::fixed_lit_len(x);
+    }
+    if (lane < 29) {
+        const long long c = s.lf[257 + lane];
+        a += c * zl::len_extra(lane);
+        f += c * zl::len_extra(lane);
+    }
+    if (lane < zl::kDistSyms) {
+        const long long c = s.df[lane];
+        a += c * (dlen[lane] + zl::dist_extra(lane));
+        f += c * (5 + zl::dist_extra(lane));
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        f += __shfl_xor_sync(0xffffffffu, f, o);
+    }
+    data = a;
+    fixed = 3 + f;
+}
+
 // Serial bit writer of lane 0 into the ring (block headers).
 struct RingW {
     uint32_t *ring;
@@ -504,6 +534,8 @@ deflate_kernel(const uint8_t *__restrict__ in, const long long *in_off, const in
             __syncwarp();  // read before the code construction overwrites the ring
             bool ok = warp_code(s, s.lf, zl::kLitSyms, s.codes.llen, lane);
             ok = warp_code(s, s.df, zl::kDistSyms, s.codes.dlen, lane) && ok;
+            long long dbits, fbits;
+            warp_block_bits(s, s.codes.llen, s.codes.dlen, lane, dbits, fbits);
             if (lane == 0) {
                 Codes &cd = s.codes;
                 for (int x = zl::kLitSyms; x < 288; ++x) cd.llen[x] = 0;
@@ -513,9 +545,9 @@ deflate_kernel(const uint8_t *__restrict__ in, const long long *in_off, const in
                     zl::canon_codes(cd.llen, 288, cd.lcode);
                     zl::canon_codes(cd.dlen, 32, cd.dcode);
                     const long long hb = zl::dynamic_header(cd);
-                    if (hb >= 0) dyn = hb + zl::data_bits(s.lf, s.df, cd.llen, cd.dlen);
+                    if (hb >= 0) dyn = hb + dbits;
                 }
-                const long long fix = zl::fixed_block_bits(s.lf, s.df);
+                const long long fix = fbits;
                 const long long sto = cov - lo <= zl::kStoredMax ? zl::stored_block_bits(rg.bp, cov - lo) : -1;
                 int mode = 2;
                 long long best = dyn;
