@@ -524,83 +524,116 @@ static inline uint32_t rd32(const uint8_t *p)
     return v;
 }
 
-/* Greedy single-pass LZ4 encoder: 4-byte hash of the current position, one
- * candidate per bucket, step acceleration over unmatched input. This is the
- * published LZ4 parsing strategy (lz4.c:337-507 follows the same scheme);
- * the bytes need not equal the reference's, only decode with its decoder. */
+/* LZ4_compress (lz4.c:695-700) restated: inputs under 65547 bytes take
+ * LZ4_compress64kCtx (lz4.c:517-673: 8192-entry table of 16-bit positions,
+ * no distance test), larger ones LZ4_compressCtx (lz4.c:337-510: 4096
+ * entries, matches at most 65535 back). Both: a zeroed table (every bucket
+ * first names position 0), the search starts at position 1, probes advance
+ * by attempts >> 6 with attempts starting at 67 at every search, and a
+ * probe is made only while the next probe position stays within the
+ * match-finder limit; a match extends backwards over equal bytes down to
+ * the anchor; after a match the table gets position-2 and the position
+ * itself is tested at once (a further match without literals, no backward
+ * extension); otherwise the next search starts one byte on. The output is
+ * byte for byte the reference's. Returns bytes written (0: cap too small). */
 int czo_lz4_compress(const uint8_t *src, int isize, uint8_t *dst, int cap)
 {
-    enum { HLOG = 12 };
-    uint32_t *tab = (uint32_t *)calloc(1u << HLOG, sizeof(uint32_t));
-    const uint8_t *ip = src, *anchor = src;
-    const uint8_t *const iend = src + isize;
-    const uint8_t *const mflimit = iend - LZ_MFLIMIT;
-    const uint8_t *const mlimit = iend - LZ_LASTLIT;
+    const int small = isize < 65536 + LZ_MFLIMIT - 1;
+    const int hlog = small ? 13 : 12;
+    uint32_t *tab = (uint32_t *)calloc(1u << hlog, sizeof(uint32_t));
+    const int mflimit = isize - LZ_MFLIMIT, mlimit = isize - LZ_LASTLIT;
+    int ip = 0, anchor = 0;
     uint8_t *op = dst, *const oend = dst + cap;
-#define HASH4(p) ((rd32(p) * 2654435761u) >> (32 - HLOG))
+#define HASHP(p) ((rd32(src + (p)) * 2654435761u) >> (32 - hlog))
+#define PUT_LEN(n)                                  \
+    do {                                            \
+        int r_ = (n);                               \
+        for (; r_ >= 255; r_ -= 255) *op++ = 255;   \
+        *op++ = (uint8_t)r_;                        \
+    } while (0)
     if (isize >= LZ_MFLIMIT + 1) {
-        tab[HASH4(ip)] = 0;
-        ip++;
+        ip = 1;
+        uint32_t fwdh = HASHP(ip);
         for (;;) {
-            const uint8_t *ref;
+            int ref, fwd = ip;
             unsigned attempts = (1u << 6) + 3;
-            for (;;) {
-                if (ip > mflimit) goto last;
-                const uint32_t h = HASH4(ip);
-                ref = src + tab[h];
-                tab[h] = (uint32_t)(ip - src);
-                if (ref < ip && ip - ref <= 65535 && rd32(ref) == rd32(ip)) break;
-                ip += attempts++ >> 6;
+            for (;;) {  /* find a match */
+                const uint32_t h = fwdh;
+                const int step = (int)(attempts++ >> 6);
+                ip = fwd;
+                fwd = ip + step;
+                if (fwd > mflimit) goto last;
+                fwdh = HASHP(fwd);
+                ref = (int)tab[h];
+                tab[h] = (uint32_t)ip;
+                if ((small || ref >= ip - 65535) && rd32(src + ref) == rd32(src + ip)) break;
             }
-            while (ip > anchor && ref > src && ip[-1] == ref[-1]) { ip--; ref--; }
-            const uint8_t *mp = ip + LZ_MINMATCH, *rp = ref + LZ_MINMATCH;
-            while (mp < mlimit && *mp == *rp) { mp++; rp++; }
-            const int lit = (int)(ip - anchor);
-            const int ml = (int)(mp - ip) - LZ_MINMATCH;
-            if (op + 1 + lit + lit / 255 + 1 + 2 + ml / 255 + 1 > oend) { free(tab); return 0; }
-            uint8_t *tok = op++;
-            if (lit >= 15) {
-                *tok = 15 << 4;
-                int r = lit - 15;
-                for (; r >= 255; r -= 255) *op++ = 255;
-                *op++ = (uint8_t)r;
-            } else {
-                *tok = (uint8_t)(lit << 4);
+            while (ip > anchor && ref > 0 && src[ip - 1] == src[ref - 1]) {
+                ip--;
+                ref--;
             }
-            memcpy(op, anchor, lit);
-            op += lit;
-            const unsigned off = (unsigned)(ip - ref);
-            *op++ = (uint8_t)off;
-            *op++ = (uint8_t)(off >> 8);
-            if (ml >= 15) {
-                *tok |= 15;
-                int r = ml - 15;
-                for (; r >= 255; r -= 255) *op++ = 255;
-                *op++ = (uint8_t)r;
-            } else {
-                *tok |= (uint8_t)ml;
+            {
+                const int lit = ip - anchor;
+                if (op + 1 + lit + lit / 255 + 1 + 2 + 8 > oend) { free(tab); return 0; }
+                uint8_t *tok = op++;
+                if (lit >= 15) {
+                    *tok = 15 << 4;
+                    PUT_LEN(lit - 15);
+                } else {
+                    *tok = (uint8_t)(lit << 4);
+                }
+                memcpy(op, src + anchor, lit);
+                op += lit;
+                for (;;) {  /* a match at ref for ip; then the position after it */
+                    const unsigned off = (unsigned)(ip - ref);
+                    *op++ = (uint8_t)off;
+                    *op++ = (uint8_t)(off >> 8);
+                    int mp = ip + LZ_MINMATCH, rp = ref + LZ_MINMATCH;
+                    while (mp < mlimit && src[mp] == src[rp]) { mp++; rp++; }
+                    const int ml = mp - ip - LZ_MINMATCH;
+                    if (op + 1 + ml / 255 + 1 + LZ_LASTLIT > oend) { free(tab); return 0; }
+                    if (ml >= 15) {
+                        *tok |= 15;
+                        PUT_LEN(ml - 15);
+                    } else {
+                        *tok |= (uint8_t)ml;
+                    }
+                    ip = mp;
+                    if (ip > mflimit) {
+                        anchor = ip;
+                        goto last;
+                    }
+                    tab[HASHP(ip - 2)] = (uint32_t)(ip - 2);
+                    const uint32_t h = HASHP(ip);
+                    ref = (int)tab[h];
+                    tab[h] = (uint32_t)ip;
+                    if ((small || ref > ip - 65536) && rd32(src + ref) == rd32(src + ip)) {
+                        if (op + 1 + 2 + 8 > oend) { free(tab); return 0; }
+                        tok = op++;
+                        *tok = 0;
+                        continue;
+                    }
+                    break;
+                }
             }
-            ip = mp;
-            anchor = ip;
-            if (ip > mflimit) break;
-            tab[HASH4(ip - 2)] = (uint32_t)(ip - 2 - src);
+            anchor = ip++;
+            fwdh = HASHP(ip);
         }
     }
 last: {
-    const int lit = (int)(iend - anchor);
+    const int lit = isize - anchor;
     if (op + 1 + lit + lit / 255 + 1 > oend) { free(tab); return 0; }
     if (lit >= 15) {
         *op++ = 15 << 4;
-        int r = lit - 15;
-        for (; r >= 255; r -= 255) *op++ = 255;
-        *op++ = (uint8_t)r;
+        PUT_LEN(lit - 15);
     } else {
         *op++ = (uint8_t)(lit << 4);
     }
-    memcpy(op, anchor, lit);
+    memcpy(op, src + anchor, lit);
     op += lit;
 }
-#undef HASH4
+#undef PUT_LEN
+#undef HASHP
     free(tab);
     return (int)(op - dst);
 }

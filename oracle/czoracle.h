@@ -2,7 +2,7 @@
  * czoracle.h -- CPU oracle for the CubismZ wavelet block codec.
  *
  * TEST INFRASTRUCTURE ONLY. This is a plain-C restatement of the reference
- * algorithm (fab4100/CubismZ, Compressor/source/*), used as the checker by
+ * algorithm (fab4100/CubismZ, Compressor/source), used as the checker by
  * tests/, by __graft_entry__.smoke() and by bench.py's CPU baseline leg. The
  * product path (libczgpu.so) never links, loads or calls it.
  *
@@ -59,9 +59,12 @@ void czo_iwt_adj_f64(double *block, int wtype);
 
 /* LZ4 legacy block format. Decoder semantics and error conventions follow
  * LZ4_uncompress_unknownOutputSize (ThirdParty/lz4/lz4.c:802-905): returns
- * the decoded length, or a value <= 0 for malformed input. */
+ * the decoded length, or minus the input position of the error (the
+ * reference decoder's values, pinned by tests/golden/lz4_cases.json). */
 int czo_lz4_decompress(const uint8_t *src, int isize, uint8_t *dst, int cap);
-/* Greedy LZ4 encoder (restated published algorithm). Returns bytes written. */
+/* LZ4_compress (ThirdParty/lz4/lz4.c:337-700) restated: the reference's
+ * bytes, pinned against its build and the committed chunks. Returns bytes
+ * written. */
 int czo_lz4_compress(const uint8_t *src, int isize, uint8_t *dst, int cap);
 int czo_lz4_bound(int isize);
 

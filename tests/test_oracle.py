@@ -65,6 +65,24 @@ def test_oracle_lz4_roundtrip_and_errors():
     assert n <= 0
 
 
+def test_oracle_lz4_compress_reproduces_reference_chunks(golden):
+    """The restated LZ4_compress gives the reference's own bytes for the
+    committed chunks (records of the small field, LZ4_compressCtx: over 64
+    KiB)."""
+    import os
+    from cubismz_gb300 import synth
+    raw, off = O.field_compress(synth.config_field("small", 0), 1e-2, 1, 4, 1, 0, 1)
+    data = open(os.path.join(os.path.dirname(__file__), "golden", "ref_lz4_chunks.bin"), "rb").read()
+    pos = 0
+    for entry in golden["ref_lz4_chunks"]:
+        zn, rn = np.frombuffer(data[pos:pos + 8], np.int32)
+        z = data[pos + 8:pos + 8 + zn]
+        pos += 8 + zn
+        chunk = raw[off[entry["chunk"]]:off[entry["chunk"] + 1]]
+        assert sha(chunk) == entry["raw_sha256"] and len(chunk) == rn
+        assert bytes(O.lz4_compress(chunk.tobytes())) == z
+
+
 def test_oracle_lz4_decoder_matches_reference_cases():
     """The restated LZ4_uncompress_unknownOutputSize returns what the
     reference's own decoder returned (output size, or minus the input
@@ -98,6 +116,23 @@ def test_oracle_equals_reference_build(zb, sh, demo_field, small_field):
                 assert np.array_equal(r, O.block_compress(b, eps, wt, zb, sh))
                 d1 = O.ref_block_decompress(L, r, wt)
                 assert np.array_equal(d1.view(np.uint32), O.block_decompress(r, wt, sh).view(np.uint32))
+
+
+@pytest.mark.skipif(ref_missing, reason="reference sources not available on this machine")
+def test_oracle_lz4_compress_equals_reference_build():
+    """The restated LZ4_compress against the reference's, byte for byte:
+    both table variants (under and over 65547 bytes), the end-of-input
+    rules, runs, random and low-entropy bytes."""
+    L = O.ref(4, 1, "lz4")
+    rng = np.random.default_rng(12)
+    cases = [b"", b"a", bytes(12), bytes(13), bytes(14), bytes(100000), rng.integers(0, 256, 70000, np.uint8).tobytes(),
+             rng.integers(0, 3, 65546, np.uint8).tobytes(), rng.integers(0, 3, 65547, np.uint8).tobytes(),
+             (b"abcdefgh" * 3000) + rng.integers(0, 4, 5000, np.uint8).tobytes()]
+    cases += [rng.integers(0, 2, n, np.uint8).tobytes() for n in range(13, 40)]
+    cases += [rng.integers(0, int(rng.integers(1, 256)), int(rng.integers(1, 3000)), np.uint8).tobytes()
+              for _ in range(40)]
+    for d in cases:
+        assert bytes(O.lz4_compress(d)) == O.ref_lz4_compress(L, d).tobytes(), len(d)
 
 
 @pytest.mark.skipif(ref_missing, reason="reference sources not available on this machine")

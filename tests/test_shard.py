@@ -102,6 +102,24 @@ def test_single_rank_file_is_the_reference_writers(lib, small_field):
         assert open(mine, "rb").read() == open(theirs, "rb").read()
 
 
+def test_single_rank_lz4_file_is_the_reference_writers(lib, small_field):
+    """Encoder lz4, 15 records per chunk, one thread: the file assembled
+    from the oracle's LZ4 chunks equals the reference writer's byte for
+    byte (the restated LZ4_compress gives the reference's bytes)."""
+    L = O.ref(4, 1, "lz4")
+    if L is None:
+        pytest.skip("reference build not available")
+    from cubismz_gb300 import api, shard
+    eps = float(np.float32(1e-3 * (small_field.max() - small_field.min())))
+    z, off = O.field_compress(small_field, eps, 1, 4, 1, 1, 15, 1)
+    part, n = shard.part_from_host(z[: off[-1]], off)
+    with tempfile.TemporaryDirectory() as d:
+        mine, theirs = os.path.join(d, "a.cz"), os.path.join(d, "b.cz")
+        shard.write_file(mine, part, n, small_field.shape, api.params(eps, 1, 4, True, "lz4", 15))
+        O.ref_write_cz(L, small_field, eps, 1, theirs, 1, 1)
+        assert open(mine, "rb").read() == open(theirs, "rb").read()
+
+
 def test_single_rank_zlib_file_is_the_reference_writers(lib, demo_field):
     """Encoder zlib, 15 records per chunk, one thread: the file assembled
     from zlib chunks equals the reference writer's byte for byte."""
