@@ -1308,9 +1308,10 @@ int cz_decompress_image(cz_ctx *c, const uint8_t *img, long long size, int wtype
         total += ps.chunk_size[i];
     }
     std::vector<long long> off(nchunks + 1);
-    for (int i = 0, acc = 0; i < nchunks; ++i) {
+    long long acc = 0;  // 64-bit: the payload of a file may pass 2 GiB
+    for (int i = 0; i < nchunks; ++i) {
         off[i] = contiguous ? ps.chunk_start[i] - ps.chunk_start[0] : acc;
-        acc += (int)ps.chunk_size[i];
+        acc += ps.chunk_size[i];
     }
     off[nchunks] = total;
     for (int i = 0; i < nchunks; ++i)
