@@ -192,3 +192,32 @@ def lz4_cases():
             data = bytes(data)
         yield data, c["cap"], c["ref"], c["sha"]
 
+
+def multi_rank_image(field, eps, world):
+    """A .cz image of `field` as `world` ranks write it (z-slabs, the
+    oracle's LZ4 chunks of one record, each rank's part, then the tail),
+    assembled in memory by the host writer functions."""
+    import ctypes as C
+    from oracle import czoracle as O
+    from cubismz_gb300 import _lib, api, shard
+    L = _lib.load()
+    nz, ny, nx = field.shape
+    parts, chunks = [], []
+    for r in range(world):
+        z0, z1 = shard.slab(nz, r, world)
+        payload, off = O.field_compress(np.ascontiguousarray(field[z0:z1]), eps, 1, 4, 1, 1, 1)
+        part, n = shard.part_from_host(payload[: off[-1]], off)
+        parts.append(part.tobytes())
+        chunks.append(n)
+    prm = api.params(eps, 1, 4, True, "lz4", 1)
+    mini = L.cz_mini_bytes()
+    hoff = mini + sum(len(p) for p in parts)
+    head = np.empty(mini, np.uint8)
+    assert L.cz_mini_write(hoff, C.c_void_p(head.ctypes.data), mini) == 0
+    tb = L.cz_tail_bytes(nx // 32, ny // 32, nz // 32, world, C.byref(prm))
+    tail = np.empty(tb, np.uint8)
+    w = C.c_longlong(0)
+    assert L.cz_tail_write(nx // 32, ny // 32, nz // 32, world, (C.c_longlong * world)(*[len(p) for p in parts]),
+                           (C.c_int * world)(*chunks), C.byref(prm), C.c_void_p(tail.ctypes.data), tb, C.byref(w)) == 0
+    return head.tobytes() + b"".join(parts) + tail[: w.value].tobytes()
+

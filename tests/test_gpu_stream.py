@@ -46,6 +46,19 @@ def test_cz_image_roundtrip(cz, small_field):
             assert np.array_equal(O.ref_read_cz(L, t.name, 1), dec)
 
 
+@pytest.mark.parametrize("world", [2, 4])
+def test_multi_rank_image_on_gpu(cz, small_field, world):
+    """A .cz image as 2 or 4 ranks write it (each rank's chunks, then its
+    LUT, then the next rank's part) decodes on the GPU to the oracle's
+    field: the reader packs the ranks' chunks before one launch."""
+    from tests.helpers import multi_rank_image
+    eps = float(np.float32(1e-3 * (small_field.max() - small_field.min())))
+    dec = cz.decompress_image(multi_rank_image(small_field, eps, world), 1, True)
+    raw, roff = O.field_compress(small_field, eps, 1, 4, 1, 0, 1)
+    want = O.field_decompress(raw, roff, small_field.shape, 1, 1)
+    assert np.array_equal(dec.view(np.uint32), want.view(np.uint32))
+
+
 def test_large_field_properties(cz):
     """512^3 (4096 blocks): per-block records equal the oracle on a sample of
     blocks, the LZ4 stage round-trips every chunk, and decompression equals

@@ -137,3 +137,30 @@ def test_single_rank_zlib_file_is_the_reference_writers(lib, demo_field):
         shard.write_file(mine, part, n, demo_field.shape, api.params(5e-5, 3, 0, False, "zlib", 15))
         O.ref_write_cz(L, demo_field, 5e-5, 3, theirs, 1, 1)
         assert open(mine, "rb").read() == open(theirs, "rb").read()
+
+
+@pytest.mark.parametrize("world", [2, 4])
+def test_in_memory_multi_rank_image(lib, small_field, world):
+    """The multi-rank image of tests.helpers.multi_rank_image (the GPU
+    reader's multi-rank test input) parses, and the reference reader decodes
+    it to the oracle's field."""
+    import ctypes as C
+    from tests.helpers import multi_rank_image
+    eps = float(np.float32(1e-3 * (small_field.max() - small_field.min())))
+    img = multi_rank_image(small_field, eps, world)
+    buf = np.frombuffer(img, np.uint8).copy()
+    dims, enc = (C.c_int * 3)(), C.c_int(-1)
+    assert lib.cz_image_info(C.c_void_p(buf.ctypes.data), len(img), dims, C.byref(enc)) == 0
+    assert list(dims) == [small_field.shape[2], small_field.shape[1], small_field.shape[0]] and enc.value == 1
+    L = O.ref(4, 1, "lz4")
+    if L is None:
+        pytest.skip("reference build not available")
+    raw, roff = O.field_compress(small_field, eps, 1, 4, 1, 0, 1)
+    want = O.field_decompress(raw, roff, small_field.shape, 1, 1)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "m.cz")
+        with open(path, "wb") as f:
+            f.write(img)
+        got = O.ref_read_cz(L, path, 1)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
