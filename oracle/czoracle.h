@@ -2,8 +2,9 @@
  * czoracle.h -- CPU oracle for the CubismZ wavelet block codec.
  *
  * TEST INFRASTRUCTURE ONLY. This is a plain-C restatement of the reference
- * algorithm (fab4100/CubismZ, Compressor/source), used as the checker by
- * tests/, by __graft_entry__.smoke() and by bench.py's CPU baseline leg. The
+ * algorithm (fab4100/CubismZ, Compressor/source) that tests/ and
+ * __graft_entry__.smoke() check the GPU results against and bench.py's CPU
+ * baseline leg runs. The
  * product path (libczgpu.so) never links, loads or calls it.
  *
  * Parity pinning: the restatement is checked bit-for-bit against the

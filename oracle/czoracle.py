@@ -1,8 +1,9 @@
 """ctypes bindings for the CPU oracle (libczoracle.so) and, where it was
 built, for the reference's own codec (oracle/_ref/libczref_<variant>.so).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg, as the checker. The product never imports it.
+TEST INFRASTRUCTURE ONLY: imported by tests/ and __graft_entry__.smoke()
+to check the GPU results, and by bench.py's CPU-baseline leg. The product
+never imports it.
 """
 import ctypes as C
 import os
