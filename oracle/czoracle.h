@@ -4,8 +4,8 @@
  * TEST INFRASTRUCTURE ONLY. This is a plain-C restatement of the reference
  * algorithm (fab4100/CubismZ, Compressor/source) that tests/ and
  * __graft_entry__.smoke() check the GPU results against and bench.py's CPU
- * baseline leg runs. The
- * product path (libczgpu.so) never links, loads or calls it.
+ * baseline leg runs. The product path (libczgpu.so) never links, loads or
+ * calls it.
  *
  * Parity pinning: the restatement is checked bit-for-bit against the
  * reference's own sources compiled in oracle/_ref (oracle/build_ref.py) on
