@@ -52,6 +52,8 @@ SIZE = 512
 REL_THR = 1e-3
 REFIT_SIZE, REFIT_THR, REFIT_ITERS = 256, 1e-3, 30
 WTYPE, ZEROBITS, SHUFFLE = 1, 4, True
+REF_MAX_THREADS, REF_BPC = 12, 15
+WORKLOAD = f"compress {SIZE}^3 fp32 field: wtype 1, thr {REL_THR}*range, zerobits 4, shuffle, lz4"
 
 
 def peaks():
@@ -344,7 +346,12 @@ def zlib_report(cz, f_dev, eps, steps):
 
 
 def refit_report(cz, dev):
-    """PSNR of the refit vs the plain path on the 256^3 refit field."""
+    """PSNR of the refit vs the plain path on the 256^3 refit field, at three
+    thresholds: the absolute 1e-3 of the config, and 1e-3 and 1e-2 of the
+    field's range (compression ratios 4 and above). Per point: the plain
+    path, the refit with the plain mask, and the refit at equal file size
+    (its threshold raised by bisection until its payload is no larger than
+    the plain one)."""
     import torch
     from cubismz_gb300 import synth
     field = synth.config_field("refit", 0)
@@ -365,45 +372,51 @@ def refit_report(cz, dev):
         cf = cz.refit_field(f, eps, REFIT_ITERS, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
         return cf.nbytes, psnr_of(cf)
 
-    eps = REFIT_THR
-    pb, pp = plain(eps)
-    rb, rp = refit(eps)
+    def point(eps, label):
+        pb, pp = plain(eps)
+        rb, rp = refit(eps)
+        lo, hi = eps, eps * 1.5
+        for _ in range(40):
+            if refit(hi)[0] <= pb:
+                break
+            lo, hi = hi, hi * 1.5
+        for _ in range(12):
+            mid = 0.5 * (lo + hi)
+            if refit(mid)[0] > pb:
+                lo = mid
+            else:
+                hi = mid
+        eb, ep = refit(hi)
+        return {"threshold": label, "eps": eps,
+                "plain": {"ratio": field.nbytes / pb, "psnr_db": pp},
+                "same_mask": {"ratio": field.nbytes / rb, "psnr_db": rp, "gain_db": rp - pp},
+                "equal_ratio": {"eps": hi, "ratio": field.nbytes / eb, "psnr_db": ep, "gain_db": ep - pp}}
+
+    pts = [point(REFIT_THR, "1e-3 absolute"),
+           point(float(np.float32(1e-3 * rng_)), "1e-3 x range"),
+           point(float(np.float32(1e-2 * rng_)), "1e-2 x range")]
+    # throughput of the refit path itself (30 CGLS steps per block)
+    refit(REFIT_THR)
     torch.cuda.synchronize()
     t = time.perf_counter()
-    refit(eps)
+    cz.refit_field(f, REFIT_THR, REFIT_ITERS, WTYPE, ZEROBITS, SHUFFLE, encoder="lz4")
     torch.cuda.synchronize()
     refit_s = time.perf_counter() - t
-    # equal file size: raise the refit threshold until its payload is no larger
-    lo, hi = eps, eps * 1.5
-    for _ in range(40):
-        if refit(hi)[0] <= pb:
-            break
-        lo, hi = hi, hi * 1.5
-    for _ in range(12):
-        mid = 0.5 * (lo + hi)
-        if refit(mid)[0] > pb:
-            lo = mid
-        else:
-            hi = mid
-    eb, ep = refit(hi)
-    return {"field": f"{REFIT_SIZE}^3 (60 blobs, 6 interfaces), thr {REFIT_THR} absolute, wtype 1, zerobits 4, "
-                     f"shuffle, lz4", "iters": REFIT_ITERS,
-            "plain": {"ratio": field.nbytes / pb, "psnr_db": pp},
-            "same_mask": {"ratio": field.nbytes / rb, "psnr_db": rp, "gain_db": rp - pp},
-            "equal_ratio": {"eps": hi, "ratio": field.nbytes / eb, "psnr_db": ep, "gain_db": ep - pp},
-            "psnr_gain_db_equal_ratio": ep - pp,
+    return {"field": f"{REFIT_SIZE}^3 (60 blobs, 6 interfaces), wtype 1, zerobits 4, shuffle, lz4",
+            "iters": REFIT_ITERS, "points": pts,
+            "psnr_gain_db_equal_ratio": pts[0]["equal_ratio"]["gain_db"],
+            "min_gain_db_equal_ratio": min(p["equal_ratio"]["gain_db"] for p in pts),
             "refit_compress_gbs": field.nbytes / refit_s / 1e9}
 
 
-def run_stress(args):
+def stress_report(dev):
     """Five 1024^3 fields (density, three velocity components, pressure;
-    ~20 GiB) from independent seeds, threshold 1e-3 x range, zero-bits 4,
-    shuffle, LZ4: compress then decompress, refit disabled and enabled
-    (same mask, so the same record bytes before LZ4)."""
+    ~20 GiB) from independent seeds, generated on the GPU, threshold 1e-3 x
+    range, zero-bits 4, shuffle, LZ4: compress then decompress, refit
+    disabled and enabled (same mask, so the same record bytes before LZ4)."""
     import torch
     import cubismz_gb300 as cz
     from cubismz_gb300 import synth
-    dev = torch.device("cuda", 0)
     names = ["density", "velocity_x", "velocity_y", "velocity_z", "pressure"]
     n = 1024
     fields = [synth.generate_torch((n, n, n), seed=5000 + i, blobs=400, interfaces=20,
@@ -414,7 +427,7 @@ def run_stress(args):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     stream = torch.cuda.current_stream(dev)
     tot_c = tot_d = 0.0
-    with Clocks(0) as clk:  # spans the five fields (their timed calls and the untimed refits)
+    with Clocks(dev.index or 0) as clk:  # spans the five fields (their timed calls and the untimed refits)
         for name, f in zip(names, fields):
             rng_ = float(f.max() - f.min())
             eps = float(np.float32(1e-3 * rng_))
@@ -445,7 +458,14 @@ def run_stress(args):
     out["compress_gbs"] = out["total_bytes"] / (tot_c * 1e-3) / 1e9
     out["decompress_gbs"] = out["total_bytes"] / (tot_d * 1e-3) / 1e9
     out["clocks"] = clk.summary()
-    print(json.dumps({"stress": out}), flush=True)
+    del fields, dec
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_stress(args):
+    import torch
+    print(json.dumps({"stress": stress_report(torch.device("cuda", 0))}), flush=True)
 
 
 def run_reference(args, rank, world):
@@ -453,16 +473,19 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     from oracle import czoracle as O
-    threads = os.cpu_count() or 1
+    # the reference's LZ4 branch allows at most 12 OpenMP threads
+    # (MAXBUFFERS, CompressionEncoders.h:197,209-212), and its writer puts 15
+    # block records in each chunk
+    threads = min(REF_MAX_THREADS, os.cpu_count() or 1)
     field = make_field(0)
     eps = float(np.float32(REL_THR * float(field.max() - field.min())))
     kind = "port"
     for _ in range(max(0, min(args.warmup, 1))):
-        O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, 1, threads)
+        O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, REF_BPC, threads)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, 1, threads)
+        O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, REF_BPC, threads)
         times.append(time.perf_counter() - t0)
     dt = float(np.mean(times))
     gbs = field.nbytes / dt / 1e9
@@ -471,11 +494,13 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"compress {SIZE}^3 fp32 field, wtype 1, thr 1e-3*range, zerobits 4, shuffle, lz4",
-                   "threads": threads},
+        "config": {"workload": WORKLOAD, "blocks_per_chunk": REF_BPC, "threads": threads,
+                   "host_cores": os.cpu_count(),
+                   "note": "12 threads: the most the reference's LZ4 branch allows (MAXBUFFERS); "
+                           "15 records per chunk as the reference writer"},
         "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": kind,
-                         "sample": f"full {SIZE}^3 field per step; the oracle port runs the reference's algorithm, "
-                                   "its LZ4_compress parse included, OpenMP over blocks",
+                         "sample": f"full {SIZE}^3 field per step, {REF_BPC} records per chunk; the oracle port runs "
+                                   "the reference's algorithm, its LZ4_compress parse included, OpenMP over blocks",
                          "gbs_by_threads": cpu_thread_counts(field, eps),
                          "by_threads_sample": f"first 64 z-planes of the {SIZE}^3 field (512 blocks)"},
         "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -590,6 +615,7 @@ def run_ours(args, rank, world, local_rank):
     zl["size_vs_lz4"] = zl["payload_bytes"] / comp_bytes
     refit = refit_report(cz, dev)
     batched = batch_report(cz, dev, max(3, args.steps))
+    stress = stress_report(dev) if not args.no_stress else None
     # ---- rooflines: the wavelet kernel and the LZ4 stage; the top-level
     # entry is the one that takes longer (the dominant kernel)
     peak, peak_kind = peaks()
@@ -619,8 +645,7 @@ def run_ours(args, rank, world, local_rank):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded 512^3 field per rank)",
-        "config": {"workload": f"compress {SIZE}^3 fp32 field per GPU: wtype 1, thr {REL_THR}*range, zerobits 4, "
-                               f"shuffle, lz4, 1 record per chunk",
+        "config": {"workload": WORKLOAD, "blocks_per_chunk": 1, "per_gpu": True,
                    "field_bytes": nbytes, "l2": "inputs larger than L2 (512 MiB field)",
                    "parallelism": f"replicas x{world}"},
         "compression": {"ratio": nbytes / image_bytes, "cz_bytes": image_bytes, "payload_bytes": comp_bytes,
@@ -639,6 +664,7 @@ def run_ours(args, rank, world, local_rank):
         "zlib": zl,
         "refit": refit,
         "batched": batched,
+        "stress": stress,
         # per compress step: encode, chunk setup, LZ4, overflow reduce, scan,
         # gather (the ncu launch list of this command shows the same six)
         "gpu_launches": 6 * args.steps,
@@ -654,6 +680,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--stress", action="store_true", help="five 1024^3 fields, refit on and off (own JSON line)")
+    ap.add_argument("--no-stress", action="store_true", help="leave the five-field stress report out of the line")
     args = ap.parse_args()
     if args.stress:
         run_stress(args)

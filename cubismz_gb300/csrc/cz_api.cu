@@ -141,6 +141,16 @@ int check_dims(cz_ctx *c, int nx, int ny, int nz)
     return CZ_OK;
 }
 
+// Device fields are read and written as float4 rows: a field pointer must
+// be 16-byte aligned (every cudaMalloc'd buffer is; an offset view may not
+// be). Checked before any launch, so a bad pointer is an error, not a fault.
+int check_align16(cz_ctx *c, const void *ptr, const char *what)
+{
+    if (reinterpret_cast<uintptr_t>(ptr) & 15u)
+        return fail(c, CZ_E_ARG, std::string(what) + " must be 16-byte aligned");
+    return CZ_OK;
+}
+
 int set_device(cz_ctx *c)
 {
     CZ_CUDA(c, cudaSetDevice(c->device));
@@ -490,6 +500,7 @@ int cz_field_compress(cz_ctx *c, const float *d_field, int nx, int ny, int nz, c
     if (!c || !d_field || !out) return fail(c, CZ_E_ARG, "NULL argument");
     CZ_TRY(check_params(c, p));
     CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(check_align16(c, d_field, "d_field"));
     CZ_TRY(set_device(c));
     const long long nblocks = (long long)(nx / 32) * (ny / 32) * (nz / 32);
     std::vector<CzField> f(1);
@@ -504,6 +515,7 @@ int cz_refit(cz_ctx *c, const float *d_field, int nx, int ny, int nz, const cz_p
     if (iters < 1 || iters > 1000) return fail(c, CZ_E_ARG, "refit iterations out of range [1, 1000]");
     CZ_TRY(check_params(c, p));
     CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(check_align16(c, d_field, "d_field"));
     CZ_TRY(set_device(c));
     const long long nblocks = (long long)(nx / 32) * (ny / 32) * (nz / 32);
     std::vector<CzField> f(1);
@@ -553,6 +565,7 @@ int cz_field_decompress(cz_ctx *c, const uint8_t *d_data, const long long *d_off
     if (!c || !d_data || !d_off || !d_field) return fail(c, CZ_E_ARG, "NULL argument");
     CZ_TRY(check_params(c, p));
     CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(check_align16(c, d_field, "d_field"));
     CZ_TRY(set_device(c));
     const long long nblocks = (long long)(nx / 32) * (ny / 32) * (nz / 32);
     const int bpc = p->blocks_per_chunk;
@@ -569,6 +582,8 @@ int cz_field_diff(cz_ctx *c, const uint8_t *d_data, const long long *d_off, int 
     if (!c || !d_data || !d_off || !d_ref || !stats) return fail(c, CZ_E_ARG, "NULL argument");
     CZ_TRY(check_params(c, p));
     CZ_TRY(check_dims(c, nx, ny, nz));
+    CZ_TRY(check_align16(c, d_ref, "d_ref"));
+    if (d_field) CZ_TRY(check_align16(c, d_field, "d_field"));
     CZ_TRY(set_device(c));
     const long long nblocks = (long long)(nx / 32) * (ny / 32) * (nz / 32);
     const int bpc = p->blocks_per_chunk;
@@ -661,6 +676,7 @@ int cz_batch_compress(cz_ctx *c, int nfields, const float *const *d_fields, cons
     for (int i = 0; i < nfields; ++i) {
         CZ_TRY(check_dims(c, dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]));
         if (!d_fields[i]) return fail(c, CZ_E_ARG, "NULL field in batch");
+        CZ_TRY(check_align16(c, d_fields[i], "every batch field"));
         f[i] = CzField{d_fields[i], dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], eps[i], total};
         total += (long long)(dims[3 * i] / 32) * (dims[3 * i + 1] / 32) * (dims[3 * i + 2] / 32);
     }
@@ -716,7 +732,8 @@ int cz_plan_create(cz_ctx *c, int nfields, const float *const *d_fields, const i
     cz_plan *pl = new cz_plan();
     long long total = 0;
     for (int i = 0; i < nfields; ++i) {
-        const int rc = check_dims(c, dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]);
+        int rc = check_dims(c, dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]);
+        if (rc == CZ_OK && d_fields[i]) rc = check_align16(c, d_fields[i], "every batch field");
         if (rc != CZ_OK || !d_fields[i]) {
             cz_plan_destroy(pl);
             return rc != CZ_OK ? rc : fail(c, CZ_E_ARG, "NULL field in batch");
@@ -1327,7 +1344,9 @@ int cz_decompress_image(cz_ctx *c, const uint8_t *img, long long size, int wtype
     } else {
         std::vector<uint8_t> packed((size_t)total);
         for (int i = 0; i < nchunks; ++i) memcpy(&packed[off[i]], img + ps.chunk_start[i], ps.chunk_size[i]);
-        CZ_CUDA(c, cudaMemcpy(d, packed.data(), (size_t)total, cudaMemcpyHostToDevice));
+        // on the call's stream: the decode kernels below run there; the
+        // synchronisation that follows keeps `packed` alive until the copy ends
+        CZ_CUDA(c, cudaMemcpyAsync(d, packed.data(), (size_t)total, cudaMemcpyHostToDevice, st));
     }
     CZ_CUDA(c, cudaMemcpyAsync(doff, off.data(), sizeof(long long) * (nchunks + 1), cudaMemcpyHostToDevice, st));
     CZ_CUDA(c, cudaStreamSynchronize(st));
@@ -1335,7 +1354,8 @@ int cz_decompress_image(cz_ctx *c, const uint8_t *img, long long size, int wtype
     f[0] = CzField{P<float>(c->tmp_field), nx, ny, nz, 0.f, 0};
     CZ_TRY(decompress_fields(c, f, nblocks, d, doff, nchunks, ps.encoder, wtype, shuffle, 1, ps.block_chunk.data(),
                              ps.block_subid.data(), std::max(1, ps.max_subid), st));
-    CZ_CUDA(c, cudaMemcpy(h_field, c->tmp_field.p, sizeof(float) * (size_t)nelem, cudaMemcpyDeviceToHost));
+    CZ_CUDA(c, cudaMemcpyAsync(h_field, c->tmp_field.p, sizeof(float) * (size_t)nelem, cudaMemcpyDeviceToHost, st));
+    CZ_CUDA(c, cudaStreamSynchronize(st));
     return CZ_OK;
 }
 

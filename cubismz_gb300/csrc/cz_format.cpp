@@ -275,7 +275,10 @@ int parse_image(const uint8_t *img, long long size, Parsed &out, std::string &er
         const int *m = &meta[5 * i];
         const long long s = i / bps;
         const int ix = m[2], iy = m[3], iz = m[4];
-        if (ix < 0 || iy < 0 || iz < 0 || ix >= out.bx || iy >= out.by || iz >= out.bz || m[0] < 0 || m[1] < 0) {
+        // a chunk holds at most its subdomain's blocks: a larger record index
+        // (subid) is damage, and would size the decode buffers by it
+        if (ix < 0 || iy < 0 || iz < 0 || ix >= out.bx || iy >= out.by || iz >= out.bz || m[0] < 0 || m[1] < 0 ||
+            m[1] >= bps) {
             err = "bad block metadata";
             return -1;
         }

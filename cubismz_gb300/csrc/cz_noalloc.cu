@@ -21,6 +21,7 @@
 // GPU (different streams, or other threads) race on it.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 
 #include "../../include/czgpu.h"
@@ -117,6 +118,12 @@ extern "C" int cz_blocks_compress_noalloc(const float *d_blocks, int nblocks, fl
 {
     if (!d_blocks || !d_records || !d_nbytes) return CZ_E_ARG;
     if (nblocks < 1 || nblocks > kMaxBlocks) return CZ_E_ARG;  // beyond the static scratch
+    // the encode kernel reads blocks as float4 rows and the copy-out writes
+    // records and sizes as 32-bit words: misaligned pointers are rejected
+    // here instead of faulting on the device
+    if ((reinterpret_cast<uintptr_t>(d_blocks) & 15u) || (reinterpret_cast<uintptr_t>(d_records) & 3u) ||
+        (reinterpret_cast<uintptr_t>(d_nbytes) & 3u))
+        return CZ_E_ARG;
     if (zerobits < 0 || zerobits > 31 || !(eps == eps)) return CZ_E_ARG;
     unsigned char *base = nullptr;
     const int rc = scratch_for_current(&base);

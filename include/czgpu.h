@@ -138,6 +138,11 @@ int cz_zlib_compress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, i
 int cz_zlib_decompress(cz_ctx *ctx, const uint8_t *src, int isize, uint8_t *dst, int cap, int *out);
 
 /* ---- field level (device buffers) ------------------------------------- */
+/* Every device field pointer of this section and of the batch, plan and
+ * refit calls (d_field, d_ref, d_fields[i]) must be 16-byte aligned: rows
+ * are read and written as 16-byte vectors. Any cudaMalloc'd buffer is; an
+ * offset view into one may not be. A misaligned pointer returns CZ_E_ARG
+ * before any work is launched. */
 /* Compress a field d_field[nz][ny][nx] (extents multiples of 32) into the
  * context's stream buffers. Asynchronous on `stream` except that it waits
  * for the stream's compressed size. Replaces the writer's _compress loop
@@ -246,7 +251,8 @@ int cz_plan_destroy(cz_plan *plan);
  * the current device. The first call on a device looks up the scratch
  * address and should come before any stream capture. Calls share the
  * scratch, so calls that overlap on the GPU race. Returns CZ_E_ARG for
- * nblocks beyond the maximum. */
+ * nblocks beyond the maximum, and when d_blocks is not 16-byte aligned or
+ * d_records or d_nbytes is not 4-byte aligned (checked before any launch). */
 #define CZ_NOALLOC_MAX_BLOCKS 16
 int cz_blocks_compress_noalloc(const float *d_blocks, int nblocks, float eps, int wtype, int zerobits, int shuffle,
                                uint8_t *d_records, int *d_nbytes, void *stream);

@@ -36,6 +36,7 @@ import io
 import json
 import lzma
 import os
+import tempfile
 import sys
 import tarfile
 
@@ -149,10 +150,11 @@ def main():
         f.write(lzma.compress(field.tobytes(), preset=9))
     gold = {"published_res": PUBLISHED}
     L = O.ref(0, 0, "zlib")
-    path = "/tmp/_cz_golden.cz"
-    O.ref_write_cz(L, field, 5e-5, 3, path, 1, 1)
-    dec = O.ref_read_cz(L, path, 3)
-    size = os.path.getsize(path)
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "demo.cz")
+        O.ref_write_cz(L, field, 5e-5, 3, path, 1, 1)
+        dec = O.ref_read_cz(L, path, 3)
+        size = os.path.getsize(path)
     gold["reference_rebuilt_res"] = res_line(field, dec, size)
     gold["reference_rebuilt_cz_bytes"] = size
     gold["reference_demo_decoded_sha256"] = sha(dec.tobytes())

@@ -50,3 +50,18 @@ def test_device_entry_points_fail_cleanly_without_gpu(lib):
     h = C.c_void_p()
     rc = lib.cz_create(0, C.byref(h))
     assert rc != 0
+
+
+def test_noalloc_pointer_checks_precede_any_cuda_call(lib):
+    """cz_blocks_compress_noalloc refuses misaligned or NULL pointers and
+    block counts beyond CZ_NOALLOC_MAX_BLOCKS with CZ_E_ARG before it touches
+    the device (these addresses are never dereferenced)."""
+    from cubismz_gb300 import _lib
+    f = lib.cz_blocks_compress_noalloc
+    ok_b, ok_r, ok_n = 0x10000, 0x20000, 0x30000
+    for b, r, n in ((ok_b + 4, ok_r, ok_n), (ok_b + 8, ok_r, ok_n), (ok_b, ok_r + 1, ok_n), (ok_b, ok_r, ok_n + 2),
+                    (0, ok_r, ok_n), (ok_b, 0, ok_n), (ok_b, ok_r, 0)):
+        assert f(C.c_void_p(b), 1, C.c_float(0.0), 1, 0, 0, C.c_void_p(r), C.c_void_p(n), None) == _lib.CZ_E_ARG
+    for nb in (0, -1, _lib.NOALLOC_MAX_BLOCKS + 1):
+        assert f(C.c_void_p(ok_b), nb, C.c_float(0.0), 1, 0, 0, C.c_void_p(ok_r), C.c_void_p(ok_n),
+                 None) == _lib.CZ_E_ARG

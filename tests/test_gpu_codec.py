@@ -113,3 +113,25 @@ def test_corrupt_records_are_rejected(cz):
     wc.compressed_data()[0] = 0xFF
     with pytest.raises(cz.CzError):
         wc.decompress(False, n - 8, 1)
+
+
+def test_misaligned_field_is_refused(cz, torch_cuda):
+    """A contiguous field view that does not start on a 16-byte boundary is
+    refused with CZ_E_ARG before any launch (rows are read as 16-byte
+    vectors), and the context keeps working."""
+    torch = torch_cuda
+    from cubismz_gb300._lib import CzError, CZ_E_ARG
+    buf = torch.zeros(32 ** 3 + 4, dtype=torch.float32, device="cuda")
+    view = buf[1:1 + 32 ** 3].view(32, 32, 32)
+    assert view.is_contiguous() and view.data_ptr() % 16 == 4
+    with pytest.raises(CzError) as e:
+        cz.compress_field(view, 1e-3, 1, 0, False, encoder="lz4")
+    assert e.value.code == CZ_E_ARG
+    good = buf[4:4 + 32 ** 3].view(32, 32, 32)
+    cf = cz.compress_field(good, 1e-3, 1, 0, False, encoder="lz4")
+    data, off = cf.to_device()
+    with pytest.raises(CzError) as e:
+        cz.decompress_field(data, off, (32, 32, 32), 1, False, encoder="lz4", out=view)
+    assert e.value.code == CZ_E_ARG
+    dec = cz.decompress_field(data, off, (32, 32, 32), 1, False, encoder="lz4").cpu().numpy()
+    assert np.array_equal(dec, np.zeros((32, 32, 32), np.float32))

@@ -137,3 +137,20 @@ def test_damaged_chunks_decode_or_fail_cleanly(gpu_lib, image, small_field):
     assert failed > 0
     assert np.array_equal(cz.decompress_image(img, 1, True).view(np.uint32), good.view(np.uint32))
 
+
+
+@pytest.mark.parametrize("subid", [64, 10 ** 6, 2 ** 31 - 1])
+def test_large_record_index_is_rejected(lib, image, subid):
+    """A block whose metadata names a record index (subid) beyond the blocks
+    of its subdomain is damage: refused before any decode buffer is sized
+    by it (the 128^3 field has 64 blocks in one subdomain)."""
+    img, _ = image
+    marker = b"==============START-BINARY-METABLOCKS==============\n"
+    m0 = img.index(marker) + len(marker)
+    b = bytearray(img)
+    b[m0 + 4:m0 + 8] = np.int32(subid).tobytes()  # BlockMetadata {chunk, subid, ix, iy, iz} of block 0
+    rc, _, _ = info(lib, b)
+    assert rc == CZ_E_CORRUPT
+    b[m0 + 4:m0 + 8] = np.int32(63).tobytes()  # in range: parses (the block's bytes are simply elsewhere)
+    rc, _, _ = info(lib, b)
+    assert rc == CZ_OK
