@@ -44,17 +44,13 @@ constexpr long long seq_bound_ll(long long n) { return 8 * (n / 4 + 2); }
 
 }  // namespace
 
-// CTAs per SM of the region LZ4 kernel (4 warps and ~64 KB of shared
-// memory each)
-constexpr int kLzRegionCtasPerSm = 3;
-
 struct cz_ctx {
     int device = 0;
     int sms = 1;
     std::string err;
     DevBuf fields, stage, rec_bytes, chunk_in, in_off, in_len, blk_dst, lz_off, lz_out, lz_len, out_off, out_data,
         queue, status, flag, rec_off, dec, dec_off, dec_cap, dec_len, raw_off, chunk_rec, block_chunk, block_subid,
-        tmp_field, tmp_in, refit, diff, zout, zoff, zlen, ierr, lz_reg;
+        tmp_field, tmp_in, refit, diff, zout, zoff, zlen, ierr;
     void *pin = nullptr;  // small pinned host scratch
     size_t pin_cap = 0;
     // geometry of the last compressed stream
@@ -193,7 +189,6 @@ void collect(cz_ctx *c)
 struct Job {
     long long nblocks = 0;
     int nfields = 0, nchunks = 0, bpc = 1, lz_warps = 4, refit_iters = 0;
-    bool lz_regions = false;  // the region-parallel LZ4 encoder (cz_lz4rec.cu)
     long long lz_slot = 0, z_slot = 0;  // per chunk: LZ4 output or DEFLATE parse; zlib output
     cz_params p{};
 };
@@ -212,11 +207,7 @@ int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, co
     job.refit_iters = refit_iters;
     const long long chunk_max = (long long)bpc * kSlotBytes;
     const bool zlib = p->encoder == CZ_ENCODER_ZLIB;
-    // one record per chunk with LZ4: the region-parallel encoder (its slot
-    // holds the regions' output areas); otherwise one warp per chunk
-    job.lz_regions = p->encoder == CZ_ENCODER_LZ4 && bpc == 1;
-    job.lz_slot = job.lz_regions ? cz_lz4rec_slot_bytes(chunk_max, bpc)
-                                 : ((zlib ? seq_bound_ll(chunk_max) : lz4_bound_ll(chunk_max)) + 15) / 16 * 16;
+    job.lz_slot = ((zlib ? seq_bound_ll(chunk_max) : lz4_bound_ll(chunk_max)) + 15) / 16 * 16;
     job.z_slot = zlib ? (zlib_bound_ll(chunk_max) + 16 + 15) / 16 * 16 : 0;
     const int nchunks = job.nchunks;
     CZ_TRY(grow(c, c->fields, sizeof(CzField) * fields.size()));
@@ -235,7 +226,6 @@ int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, co
         CZ_TRY(grow(c, c->chunk_in, (size_t)nchunks * bpc * kSlotBytes));
     }
     if (p->encoder != CZ_ENCODER_NONE) CZ_TRY(grow(c, c->lz_out, (size_t)nchunks * job.lz_slot));
-    if (job.lz_regions) CZ_TRY(grow(c, c->lz_reg, sizeof(LzRegion) * 3 * (size_t)bpc * nchunks));
     if (zlib) {
         CZ_TRY(grow(c, c->zout, (size_t)nchunks * job.z_slot));
         CZ_TRY(grow(c, c->zoff, sizeof(long long) * nchunks));
@@ -285,25 +275,7 @@ int enqueue(cz_ctx *c, const Job &job, cudaStream_t st, bool marks)
     const uint8_t *gsrc = chunk_src;
     const long long *gsrc_off = P<long long>(c->in_off);
     const int *glen = P<int>(c->in_len);
-    if (job.lz_regions) {
-        // a warp per record region, then the joined blocks' sizes; the
-        // stitch below writes them (in place of the gather)
-        const int rgrid = std::max(1, std::min((3 * nchunks + 3) / 4, c->sms * kLzRegionCtasPerSm));
-        CZ_CUDA(c, cz_launch_lz4_regions(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
-                                         P<int>(c->rec_bytes), nullptr, nblocks, 1, p->shuffle ? 1 : 0,
-                                         P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<LzRegion>(c->lz_reg),
-                                         rgrid, st));
-        CZ_CUDA(c, cz_launch_lz4_region_sizes(P<LzRegion>(c->lz_reg), P<int>(c->in_len), nchunks, 1,
-                                              P<int>(c->lz_len), st));
-        CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len), nchunks, P<int>(c->flag), st));
-        if (marks) CZ_TRY(mark(c, 2, st));
-        CZ_CUDA(c, cz_launch_scan(P<int>(c->lz_len), nchunks, P<long long>(c->out_off), st));
-        CZ_CUDA(c, cz_launch_lz4_stitch(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks, 1,
-                                        P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<LzRegion>(c->lz_reg),
-                                        P<uint8_t>(c->out_data), P<long long>(c->out_off), st));
-        if (marks) CZ_TRY(mark(c, 3, st));
-        return CZ_OK;
-    } else if (p->encoder == CZ_ENCODER_LZ4) {
+    if (p->encoder == CZ_ENCODER_LZ4) {
         const int per = job.lz_warps;
         const int lzgrid = std::max(1, std::min((nchunks + per - 1) / per, c->sms * (32 / per)));
         CZ_CUDA(c, cz_launch_lz4_encode(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
@@ -488,7 +460,7 @@ int cz_destroy(cz_ctx *c)
                      &c->blk_dst, &c->lz_off,  &c->lz_out,    &c->lz_len,    &c->out_off,     &c->out_data,
                      &c->queue,   &c->status,  &c->flag,      &c->rec_off,   &c->dec,         &c->dec_off,
                      &c->dec_cap, &c->dec_len, &c->raw_off,   &c->chunk_rec, &c->block_chunk, &c->block_subid,
-                     &c->tmp_field, &c->tmp_in, &c->lz_reg};
+                     &c->tmp_field, &c->tmp_in};
     for (DevBuf *b : all)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->ev)
@@ -1202,26 +1174,6 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
         const long long *src_off = P<long long>(c->in_off) + f0;
         const int *len = P<int>(c->in_len) + f0;
         cudaEvent_t ready = c->ev_enc[i];
-        if (lz4 && job.lz_regions) {
-            cudaStream_t ls = c->s_lz[i];
-            CZ_CUDA(c, cudaStreamWaitEvent(ls, c->ev_enc[i], 0));
-            const int rgrid = std::max(1, std::min((3 * n + 3) / 4, c->sms * kLzRegionCtasPerSm));
-            // the slab's chunk offsets (input and output) are slab-relative
-            uint8_t *lzo = P<uint8_t>(c->lz_out) + f0 * job.lz_slot;
-            CZ_CUDA(c, cz_launch_lz4_regions(stage, src_off, len, n, P<int>(c->rec_bytes) + f0, nullptr, n, 1,
-                                             p->shuffle ? 1 : 0, lzo, P<long long>(c->lz_off) + f0,
-                                             P<LzRegion>(c->lz_reg) + 3 * f0, rgrid, ls));
-            CZ_CUDA(c, cz_launch_lz4_region_sizes(P<LzRegion>(c->lz_reg) + 3 * f0, len, n, 1,
-                                                  P<int>(c->lz_len) + f0, ls));
-            CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len) + f0, n, P<int>(c->flag), ls));
-            CZ_CUDA(c, cudaEventRecord(c->ev_lz[i], ls));
-            CZ_CUDA(c, cudaStreamWaitEvent(c->s_gather, c->ev_lz[i], 0));
-            CZ_CUDA(c, cz_launch_scan_from(P<int>(c->lz_len) + f0, n, P<long long>(c->out_off) + f0, c->s_gather));
-            CZ_CUDA(c, cz_launch_lz4_stitch(stage, src_off, len, n, 1, lzo,
-                                            P<long long>(c->lz_off) + f0, P<LzRegion>(c->lz_reg) + 3 * f0, dst,
-                                            P<long long>(c->out_off) + f0, c->s_gather));
-            continue;
-        }
         if (lz4) {
             cudaStream_t ls = c->s_lz[i];
             CZ_CUDA(c, cudaStreamWaitEvent(ls, c->ev_enc[i], 0));
