@@ -166,6 +166,32 @@ __device__ __forceinline__ void w_apply(float *sb)
     lsweep<32, 1, false, KIND>(sb);
     lsweep<32, 0, false, KIND>(sb);
 }
+// W, returning this thread's part of ||W v||^2: the last sweep (x lines of
+// level 32) sums the squares of the lines it writes.
+template <int KIND>
+__device__ __forceinline__ float w_apply_norm(float *sb)
+{
+    lsweep<8, 0, false, KIND>(sb);
+    lsweep<8, 2, false, KIND>(sb);
+    lsweep<8, 1, false, KIND>(sb);
+    lsweep<16, 1, false, KIND>(sb);
+    lsweep<16, 0, false, KIND>(sb);
+    lsweep<16, 2, false, KIND>(sb);
+    lsweep<32, 2, false, KIND>(sb);
+    lsweep<32, 1, false, KIND>(sb);
+    float acc = 0.f;
+    for (int l = threadIdx.x; l < 32 * 32; l += kNT) {
+        const int base = line_base<32, 0>(l);
+        float v[32];
+        ld_line<32, 0>(sb, base, v);
+        lin_inv<32, KIND>(v);
+        st_line<32, 0>(sb, base, v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc = __fmaf_rn(v[j], v[j], acc);
+    }
+    __syncthreads();
+    return acc;
+}
 template <int KIND>
 __device__ __forceinline__ void wt_apply(float *sb)
 {
@@ -323,75 +349,151 @@ refit_kernel(const CzField *fields, int nfields, long long total_blocks, int zer
             emit8(s, y, z, keep_bits<8>(v, eps));
         }
         __syncthreads();
-        // keep bit of kernel-layout element i (x fastest)
-        auto keep = [&](int i) -> bool {
-            const int m = mask_index(i & 31, (i >> 5) & 31, i >> 10);
-            return (s.mask32[m >> 5] >> (m & 31)) & 1u;
-        };
-        // ---- c0 = M c_full; r = x - W c0; s = M W^T r; p = s
-        for (int i = threadIdx.x; i < kBS3; i += kNT) {
-            const int a = pad_of(i);
-            const float v = keep(i) ? sb[a] : 0.f;
-            sb[a] = v;
-            Cv[i] = v;
+        // The element passes below work on 4 consecutive elements (x
+        // fastest) per thread and step: 16-byte loads and stores of the
+        // iterates, several in flight per thread (the iterates live in L2).
+        // Keep bits of elements i0 .. i0+3 (bit e for i0 + e).
+        // The keep bits in kernel layout (word y + 32 z, bit x), built once
+        // per block by warp votes into the emission stage, which is idle
+        // until the record is written.
+        uint32_t *km = reinterpret_cast<uint32_t *>(s.stage);
+        for (int row = threadIdx.x >> 5; row < 1024; row += kNW) {
+            const int x = threadIdx.x & 31, m = mask_index(x, row & 31, row >> 5);
+            const unsigned w = __ballot_sync(0xffffffffu, (s.mask32[m >> 5] >> (m & 31)) & 1u);
+            if (x == 0) km[row] = w;
+        }
+        __syncthreads();
+        auto keep4 = [&](int i0) -> unsigned { return (km[i0 >> 5] >> (i0 & 31)) & 0xFu; };
+        float4 *C4 = reinterpret_cast<float4 *>(Cv), *P4 = reinterpret_cast<float4 *>(Pv),
+               *R4 = reinterpret_cast<float4 *>(Rv);
+        constexpr int kV = kBS3 / 4;
+        // ---- c0 = M c_full; r = x - W c0; s = M W^T r; p = s (also in sb)
+#pragma unroll 4
+        for (int j = threadIdx.x; j < kV; j += kNT) {
+            const int i0 = 4 * j, a = pad_of(i0);
+            const unsigned k = keep4(i0);
+            float4 v;
+            v.x = (k & 1u) ? sb[a] : 0.f;
+            v.y = (k & 2u) ? sb[a + 1] : 0.f;
+            v.z = (k & 4u) ? sb[a + 2] : 0.f;
+            v.w = (k & 8u) ? sb[a + 3] : 0.f;
+            sb[a] = v.x;
+            sb[a + 1] = v.y;
+            sb[a + 2] = v.z;
+            sb[a + 3] = v.w;
+            C4[j] = v;
         }
         __syncthreads();
         w_apply<KIND>(sb);
-        for (int i = threadIdx.x; i < kBS3; i += kNT) {
-            const int a = pad_of(i);
-            const float xv = __ldg(ref.f->data + row_offset(ref, (i >> 5) & 31, i >> 10) + (i & 31));
-            const float r = xv - sb[a];
-            Rv[i] = r;
-            sb[a] = r;
+#pragma unroll 4
+        for (int j = threadIdx.x; j < kV; j += kNT) {
+            const int i0 = 4 * j, a = pad_of(i0);
+            const float4 xv =
+                __ldg(reinterpret_cast<const float4 *>(ref.f->data + row_offset(ref, (i0 >> 5) & 31, i0 >> 10)) +
+                      ((i0 & 31) >> 2));
+            float4 r;
+            r.x = xv.x - sb[a];
+            r.y = xv.y - sb[a + 1];
+            r.z = xv.z - sb[a + 2];
+            r.w = xv.w - sb[a + 3];
+            R4[j] = r;
+            sb[a] = r.x;
+            sb[a + 1] = r.y;
+            sb[a + 2] = r.z;
+            sb[a + 3] = r.w;
         }
         __syncthreads();
         wt_apply<KIND>(sb);
-        double acc = 0;
-        for (int i = threadIdx.x; i < kBS3; i += kNT) {
-            const float v = keep(i) ? sb[pad_of(i)] : 0.f;
-            Pv[i] = v;
-            acc += (double)v * v;
+        float acc = 0.f;
+#pragma unroll 4
+        for (int j = threadIdx.x; j < kV; j += kNT) {
+            const int i0 = 4 * j, a = pad_of(i0);
+            const unsigned k = keep4(i0);
+            float4 v;
+            v.x = (k & 1u) ? sb[a] : 0.f;
+            v.y = (k & 2u) ? sb[a + 1] : 0.f;
+            v.z = (k & 4u) ? sb[a + 2] : 0.f;
+            v.w = (k & 8u) ? sb[a + 3] : 0.f;
+            sb[a] = v.x;
+            sb[a + 1] = v.y;
+            sb[a + 2] = v.z;
+            sb[a + 3] = v.w;
+            P4[j] = v;
+            acc = __fmaf_rn(v.x, v.x, __fmaf_rn(v.y, v.y, __fmaf_rn(v.z, v.z, __fmaf_rn(v.w, v.w, acc))));
         }
-        double gamma = block_sum(acc, red);
+        double gamma = block_sum(acc, red);  // its barriers also order sb for W
         for (int it = 0; it < iters && gamma > 0.0; ++it) {
-            // q = W p
-            for (int i = threadIdx.x; i < kBS3; i += kNT) sb[pad_of(i)] = Pv[i];
-            __syncthreads();
-            w_apply<KIND>(sb);
-            acc = 0;
-            for (int i = threadIdx.x; i < kBS3; i += kNT) {
-                const float q = sb[pad_of(i)];
-                acc += (double)q * q;
-            }
+            // q = W p (sb holds p); ||q||^2 from the last sweep's lines
+            acc = w_apply_norm<KIND>(sb);
             const double delta = block_sum(acc, red);
             if (!(delta > 0.0)) break;
             const float alpha = (float)(gamma / delta);
-            // c += alpha p; r -= alpha q
-            for (int i = threadIdx.x; i < kBS3; i += kNT) {
-                const int a = pad_of(i);
-                Cv[i] = __fmaf_rn(alpha, Pv[i], Cv[i]);
-                const float r = __fmaf_rn(-alpha, sb[a], Rv[i]);
-                Rv[i] = r;
-                sb[a] = r;
+            // c += alpha p; r -= alpha q (sb gets r)
+#pragma unroll 4
+            for (int j = threadIdx.x; j < kV; j += kNT) {
+                const int a = pad_of(4 * j);
+                const float4 pv = P4[j];
+                float4 cv = C4[j], rv = R4[j];
+                cv.x = __fmaf_rn(alpha, pv.x, cv.x);
+                cv.y = __fmaf_rn(alpha, pv.y, cv.y);
+                cv.z = __fmaf_rn(alpha, pv.z, cv.z);
+                cv.w = __fmaf_rn(alpha, pv.w, cv.w);
+                rv.x = __fmaf_rn(-alpha, sb[a], rv.x);
+                rv.y = __fmaf_rn(-alpha, sb[a + 1], rv.y);
+                rv.z = __fmaf_rn(-alpha, sb[a + 2], rv.z);
+                rv.w = __fmaf_rn(-alpha, sb[a + 3], rv.w);
+                C4[j] = cv;
+                R4[j] = rv;
+                sb[a] = rv.x;
+                sb[a + 1] = rv.y;
+                sb[a + 2] = rv.z;
+                sb[a + 3] = rv.w;
             }
             __syncthreads();
-            // s = M W^T r; p = s + beta p
+            // s = M W^T r; p = s + beta p (sb gets p for the next W)
             wt_apply<KIND>(sb);
-            acc = 0;
-            for (int i = threadIdx.x; i < kBS3; i += kNT) {
-                const int a = pad_of(i);
-                const float v = keep(i) ? sb[a] : 0.f;
-                sb[a] = v;
-                acc += (double)v * v;
+            acc = 0.f;
+#pragma unroll 4
+            for (int j = threadIdx.x; j < kV; j += kNT) {
+                const int i0 = 4 * j, a = pad_of(i0);
+                const unsigned k = keep4(i0);
+                const float v0 = (k & 1u) ? sb[a] : 0.f, v1 = (k & 2u) ? sb[a + 1] : 0.f,
+                            v2 = (k & 4u) ? sb[a + 2] : 0.f, v3 = (k & 8u) ? sb[a + 3] : 0.f;
+                sb[a] = v0;
+                sb[a + 1] = v1;
+                sb[a + 2] = v2;
+                sb[a + 3] = v3;
+                acc = __fmaf_rn(v0, v0, __fmaf_rn(v1, v1, __fmaf_rn(v2, v2, __fmaf_rn(v3, v3, acc))));
             }
             const double gnew = block_sum(acc, red);
             const float beta = (float)(gnew / gamma);
-            for (int i = threadIdx.x; i < kBS3; i += kNT) Pv[i] = __fmaf_rn(beta, Pv[i], sb[pad_of(i)]);
+#pragma unroll 4
+            for (int j = threadIdx.x; j < kV; j += kNT) {
+                const int a = pad_of(4 * j);
+                float4 pv = P4[j];
+                pv.x = __fmaf_rn(beta, pv.x, sb[a]);
+                pv.y = __fmaf_rn(beta, pv.y, sb[a + 1]);
+                pv.z = __fmaf_rn(beta, pv.z, sb[a + 2]);
+                pv.w = __fmaf_rn(beta, pv.w, sb[a + 3]);
+                P4[j] = pv;
+                sb[a] = pv.x;
+                sb[a + 1] = pv.y;
+                sb[a + 2] = pv.z;
+                sb[a + 3] = pv.w;
+            }
             gamma = gnew;
             __syncthreads();
         }
         // ---- the refit survivors go out under the plain mask
-        for (int i = threadIdx.x; i < kBS3; i += kNT) sb[pad_of(i)] = Cv[i];
+#pragma unroll 4
+        for (int j = threadIdx.x; j < kBS3 / 4; j += kNT) {
+            const int a = pad_of(4 * j);
+            const float4 cv = reinterpret_cast<const float4 *>(Cv)[j];
+            sb[a] = cv.x;
+            sb[a + 1] = cv.y;
+            sb[a + 2] = cv.z;
+            sb[a + 3] = cv.w;
+        }
         __syncthreads();
         emit_record(s, g, zmask, shuffle, stage, rec_bytes);
     }
