@@ -85,8 +85,10 @@ __device__ __forceinline__ void encode_body(const CzField *fields, int nfields, 
             emit32(s, x, y, keep_bits<32>(v, eps));
         }
         __syncthreads();
-        // the next block's rows load while this one finishes
-        if (gn < total_blocks) load_rows(locate(fields, nfields, gn), pf);
+        // the next block's rows load while this one finishes: the warps
+        // that level 16 leaves idle (threads >= 256) now, the others once
+        // level 16 is done
+        if (threadIdx.x >= 256 && gn < total_blocks) load_rows(locate(fields, nfields, gn), pf);
         // ---- level 16 (z, x, y) on the [0,16)^3 corner
         sweep<16, 2, true, KIND>(s.sb);
         __syncthreads();
@@ -102,6 +104,7 @@ __device__ __forceinline__ void encode_body(const CzField *fields, int nfields, 
             emit16(s, x, z, keep_bits<16>(v, eps));
         }
         __syncthreads();
+        if (threadIdx.x < 256 && gn < total_blocks) load_rows(locate(fields, nfields, gn), pf);
         // ---- level 8 (y, z, x) on the [0,8)^3 corner
         sweep<8, 1, true, KIND>(s.sb);
         __syncthreads();
