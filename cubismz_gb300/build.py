@@ -19,7 +19,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libczgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["cz_codec.cu", "cz_lz4.cu", "cz_lz4rec.cu", "cz_stream.cu", "cz_api.cu", "cz_noalloc.cu", "cz_refit.cu", "cz_ingest.cu", "cz_zlib.cu", "cz_format.cpp"]
+SOURCES = ["cz_codec.cu", "cz_lz4.cu", "cz_stream.cu", "cz_api.cu", "cz_noalloc.cu", "cz_refit.cu", "cz_ingest.cu", "cz_zlib.cu", "cz_format.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "--expt-relaxed-constexpr"]

@@ -44,17 +44,13 @@ constexpr long long seq_bound_ll(long long n) { return 8 * (n / 4 + 2); }
 
 }  // namespace
 
-// slabs at the end of the pipelined image path that take the
-// region-parallel LZ4 encoder
-constexpr int kRegionSlabs = 2;
-
 struct cz_ctx {
     int device = 0;
     int sms = 1;
     std::string err;
     DevBuf fields, stage, rec_bytes, chunk_in, in_off, in_len, blk_dst, lz_off, lz_out, lz_len, out_off, out_data,
         queue, status, flag, rec_off, dec, dec_off, dec_cap, dec_len, raw_off, chunk_rec, block_chunk, block_subid,
-        tmp_field, tmp_in, refit, diff, zout, zoff, zlen, ierr, lz_reg;
+        tmp_field, tmp_in, refit, diff, zout, zoff, zlen, ierr;
     void *pin = nullptr;  // small pinned host scratch
     size_t pin_cap = 0;
     // geometry of the last compressed stream
@@ -212,11 +208,6 @@ int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, co
     const long long chunk_max = (long long)bpc * kSlotBytes;
     const bool zlib = p->encoder == CZ_ENCODER_ZLIB;
     job.lz_slot = ((zlib ? seq_bound_ll(chunk_max) : lz4_bound_ll(chunk_max)) + 15) / 16 * 16;
-    // one record per chunk with LZ4: the slots also hold the region areas of
-    // the region-parallel encoder (used for the last slabs of the pipelined
-    // image path)
-    if (p->encoder == CZ_ENCODER_LZ4 && bpc == 1)
-        job.lz_slot = std::max(job.lz_slot, cz_lz4rec_slot_bytes(chunk_max, 1));
     job.z_slot = zlib ? (zlib_bound_ll(chunk_max) + 16 + 15) / 16 * 16 : 0;
     const int nchunks = job.nchunks;
     CZ_TRY(grow(c, c->fields, sizeof(CzField) * fields.size()));
@@ -235,7 +226,6 @@ int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, co
         CZ_TRY(grow(c, c->chunk_in, (size_t)nchunks * bpc * kSlotBytes));
     }
     if (p->encoder != CZ_ENCODER_NONE) CZ_TRY(grow(c, c->lz_out, (size_t)nchunks * job.lz_slot));
-    if (p->encoder == CZ_ENCODER_LZ4 && bpc == 1) CZ_TRY(grow(c, c->lz_reg, sizeof(LzRegion) * 3 * (size_t)nchunks));
     if (zlib) {
         CZ_TRY(grow(c, c->zout, (size_t)nchunks * job.z_slot));
         CZ_TRY(grow(c, c->zoff, sizeof(long long) * nchunks));
@@ -470,7 +460,7 @@ int cz_destroy(cz_ctx *c)
                      &c->blk_dst, &c->lz_off,  &c->lz_out,    &c->lz_len,    &c->out_off,     &c->out_data,
                      &c->queue,   &c->status,  &c->flag,      &c->rec_off,   &c->dec,         &c->dec_off,
                      &c->dec_cap, &c->dec_len, &c->raw_off,   &c->chunk_rec, &c->block_chunk, &c->block_subid,
-                     &c->tmp_field, &c->tmp_in, &c->lz_reg};
+                     &c->tmp_field, &c->tmp_in};
     for (DevBuf *b : all)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->ev)
@@ -1169,7 +1159,6 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
         CZ_CUDA(c, cudaEventRecord(c->ev_h2d[i], c->s_copy));
     }
     unsigned long long *queues = P<unsigned long long>(c->queue);
-    const int lzr_warps = cz_lz4rec_warps_per_cta();
     for (int i = 0; i < nslab; ++i) {
         const long long f0 = first[i];
         const int n = (int)(first[i + 1] - f0);
@@ -1185,26 +1174,6 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
         const long long *src_off = P<long long>(c->in_off) + f0;
         const int *len = P<int>(c->in_len) + f0;
         cudaEvent_t ready = c->ev_enc[i];
-        if (lz4 && i >= nslab - kRegionSlabs) {
-            // the last slabs: the region-parallel encoder (a warp per record
-            // region, a third of a chunk's parse latency), so that the work
-            // left after the last host-to-device copy ends sooner
-            cudaStream_t ls = c->s_lz[i];
-            CZ_CUDA(c, cudaStreamWaitEvent(ls, c->ev_enc[i], 0));
-            uint8_t *lzo = P<uint8_t>(c->lz_out) + f0 * job.lz_slot;  // slab-relative offsets
-            LzRegion *reg = P<LzRegion>(c->lz_reg) + 3 * f0;
-            const int rgrid = std::max(1, (3 * n + lzr_warps - 1) / lzr_warps);
-            CZ_CUDA(c, cz_launch_lz4_regions(stage, src_off, len, n, P<int>(c->rec_bytes) + f0, nullptr, n, 1,
-                                             p->shuffle ? 1 : 0, lzo, P<long long>(c->lz_off) + f0, reg, rgrid, ls));
-            CZ_CUDA(c, cz_launch_lz4_region_sizes(reg, len, n, 1, P<int>(c->lz_len) + f0, ls));
-            CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len) + f0, n, P<int>(c->flag), ls));
-            CZ_CUDA(c, cudaEventRecord(c->ev_lz[i], ls));
-            CZ_CUDA(c, cudaStreamWaitEvent(c->s_gather, c->ev_lz[i], 0));
-            CZ_CUDA(c, cz_launch_scan_from(P<int>(c->lz_len) + f0, n, P<long long>(c->out_off) + f0, c->s_gather));
-            CZ_CUDA(c, cz_launch_lz4_stitch(stage, src_off, len, n, 1, lzo, P<long long>(c->lz_off) + f0, reg, dst,
-                                            P<long long>(c->out_off) + f0, c->s_gather));
-            continue;
-        }
         if (lz4) {
             cudaStream_t ls = c->s_lz[i];
             CZ_CUDA(c, cudaStreamWaitEvent(ls, c->ev_enc[i], 0));

@@ -53,38 +53,6 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
                                  int grid, cudaStream_t st);
-// LZ4 of block-record chunks, region-parallel (cz_lz4rec.cu). Chunk c holds
-// the records of blocks [c*bpc, (c+1)*bpc) ([int32 nbytes][record] each, at
-// blk_dst[g] inside the chunk input, or at in_off[c] when blk_dst is NULL
-// and bpc = 1). Three regions per record (header and mask; byte plane 0, or
-// the payload without shuffle; byte plane 3) are parsed by one warp each
-// into the chunk's slot at out + out_off[c] (cz_lz4rec_slot_bytes(chunk
-// bytes, bpc) per chunk); reg[c*3*bpc + region] describes them. The sizes
-// kernel gives each chunk's LZ4 block size (-1: a region overflowed its
-// area, which the slot size rules out); the stitch kernel writes the
-// blocks at dst + dst_off[c]. Chunk inputs are read as aligned words up to
-// 4 bytes past their end.
-struct LzRegion {
-    int a;          // region start (chunk position)
-    int first_st;   // start of the region's first match, -1: none
-    int first_hdr;  // bytes of its first sequence's token and literal length
-    int last_end;   // end of its last match
-    int rbytes;     // output bytes, -1 on overflow
-    int ridx;       // region index within the chunk
-    int pad0, pad1;
-};
-int cz_lz4rec_smem_bytes(void);
-int cz_lz4rec_warps_per_cta(void);
-long long cz_lz4rec_slot_bytes(long long chunk_max, int bpc);
-cudaError_t cz_launch_lz4_regions(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
-                                  const int *rec_bytes, const long long *blk_dst, long long nblocks, int bpc,
-                                  int shuffle, uint8_t *out, const long long *out_off, LzRegion *reg, int grid,
-                                  cudaStream_t st);
-cudaError_t cz_launch_lz4_region_sizes(const LzRegion *reg, const int *in_len, int nchunks, int bpc, int *out_len,
-                                       cudaStream_t st);
-cudaError_t cz_launch_lz4_stitch(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks, int bpc,
-                                 const uint8_t *lz, const long long *lz_off, const LzRegion *reg, uint8_t *out,
-                                 const long long *dst_off, cudaStream_t st);
 // The LZ77 parse of the LZ4 encoder for DEFLATE: distances up to 32 KiB,
 // 8-byte sequence records (zl::seq_pack) per chunk at seq + seq_off[c]
 // (capacity 8 * (in_len/4 + 2) bytes); seq_bytes[c] = record bytes.
