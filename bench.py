@@ -279,8 +279,10 @@ def batch_report(cz, dev, steps):
            "thresholds": "log-uniform [1e-5, 1e-2] x field range", "ms_per_step": ms,
            "value": total / (ms * 1e-3) / 1e9, "unit": "GB/s", "ratio": total / cf.nbytes,
            "graph": "one cudaGraphLaunch per step (persistent wavelet kernel over all fields, LZ4, assembly)",
-           "autotune": {"lz4_warps_per_cta": info["lz4_warps_per_cta"],
-                        "lz4_stage_ms": {str(k): v for k, v in info["tune_ms"].items()}}}
+           "autotune": {"space": "LZ4 chunks per CTA {2, 4, 8, 16} x wavelet-kernel row prefetch {split, joint}",
+                        "chosen": info["shape"],
+                        "lz4_stage_ms": {str(k): v for k, v in info["lz4_stage_ms"].items()},
+                        "wavelet_kernel_ms": info["wavelet_kernel_ms"]}}
     plan.close()
     del fields
     torch.cuda.empty_cache()

@@ -34,7 +34,7 @@ EXPORTS = [
     "cz_blocks_compress_noalloc", "cz_iwt_linear", "cz_iwt_adjoint", "cz_refit",
     "cz_mini_bytes", "cz_mini_write", "cz_part_bytes", "cz_part_write", "cz_stream_part", "cz_tail_bytes",
     "cz_tail_write", "cz_plan_create", "cz_plan_launch", "cz_plan_result", "cz_plan_info", "cz_plan_last_error",
-    "cz_plan_destroy", "cz_field_diff", "cz_res_line", "cz_field_from_zfastest", "cz_field_to_zfastest",
+    "cz_plan_destroy", "cz_plan_shape", "cz_field_diff", "cz_res_line", "cz_field_from_zfastest", "cz_field_to_zfastest",
     "cz_zlib_decompress", "cz_zlib_bound", "cz_zlib_compress",
 ]
 NOALLOC_MAX_BLOCKS = 16
@@ -110,6 +110,7 @@ def load():
                                  C.POINTER(C.c_void_p)]
     L.cz_plan_launch.argtypes = [vp, vp]
     L.cz_plan_result.argtypes = [vp, vp, C.POINTER(Stream), C.POINTER(Stream)]
+    L.cz_plan_shape.argtypes = [vp, ip, fp]
     L.cz_plan_info.argtypes = [vp, ip, fp]
     L.cz_plan_last_error.argtypes = [vp]
     L.cz_plan_last_error.restype = C.c_char_p

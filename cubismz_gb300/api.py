@@ -295,7 +295,13 @@ class Plan:
         w = C.c_int(0)
         t = (C.c_float * 3)()
         self.ctx.L.cz_plan_info(self.h, C.byref(w), t)
-        return {"lz4_warps_per_cta": w.value, "tune_ms": {2: t[0], 4: t[1], 8: t[2]}}
+        shape = (C.c_int * 2)()
+        ms = (C.c_float * 6)()
+        self.ctx.L.cz_plan_shape(self.h, shape, ms)
+        return {"lz4_warps_per_cta": w.value, "tune_ms": {2: t[0], 4: t[1], 8: t[2]},
+                "shape": {"lz4_chunks_per_cta": shape[0], "wavelet_variant": shape[1]},
+                "lz4_stage_ms": {2: ms[0], 4: ms[1], 8: ms[2], 16: ms[3]},
+                "wavelet_kernel_ms": {"split_prefetch": ms[4], "joint_prefetch": ms[5]}}
 
     def close(self):
         if self.h:

@@ -188,7 +188,7 @@ void collect(cz_ctx *c)
 //   finish   waits for the stream, reads the totals, fills *out.
 struct Job {
     long long nblocks = 0;
-    int nfields = 0, nchunks = 0, bpc = 1, lz_warps = 4, refit_iters = 0;
+    int nfields = 0, nchunks = 0, bpc = 1, lz_warps = 4, refit_iters = 0, enc_variant = 0;
     long long lz_slot = 0, z_slot = 0;  // per chunk: LZ4 output or DEFLATE parse; zlib output
     cz_params p{};
 };
@@ -260,7 +260,7 @@ int enqueue(cz_ctx *c, const Job &job, cudaStream_t st, bool marks)
     else
         CZ_CUDA(c, cz_launch_encode(p->wtype, P<CzField>(c->fields), job.nfields, nblocks, p->zerobits,
                                     p->shuffle ? 1 : 0, P<uint8_t>(c->stage), P<int>(c->rec_bytes),
-                                    P<unsigned long long>(c->queue), grid, st));
+                                    P<unsigned long long>(c->queue), grid, st, job.enc_variant));
     if (marks) CZ_TRY(mark(c, 1, st));
     CZ_CUDA(c, cz_launch_chunk_setup(bpc, nblocks, nchunks, P<int>(c->rec_bytes), P<long long>(c->in_off),
                                      P<int>(c->in_len), bpc > 1 ? P<long long>(c->blk_dst) : nullptr,
@@ -707,7 +707,10 @@ struct cz_plan {
     cudaStream_t st = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    float tune_ms[3] = {-1.f, -1.f, -1.f};  // LZ4 stage per candidate: 2, 4, 8 warps per CTA
+    // autotuner timings (-1: not tuned): the LZ4 stage at 2, 4, 8, 16 chunks
+    // per CTA, the wavelet kernel in its two row-prefetch variants
+    float lz_ms[4] = {-1.f, -1.f, -1.f, -1.f};
+    float enc_ms[2] = {-1.f, -1.f};
 };
 
 int cz_plan_destroy(cz_plan *pl)
@@ -758,31 +761,47 @@ int cz_plan_create(cz_ctx *c, int nfields, const float *const *d_fields, const i
         return bail(CZ_E_CUDA, "plan stream");
     }
     if ((rc = prepare(pl->c, f, total, &q, 0, pl->st, pl->job)) != CZ_OK) return bail(rc, "prepare");
-    // autotuner: the LZ4 stage's CTA shape (chunks per CTA), timed on this
-    // batch; every shape writes the same bytes
+    // autotuner, timed on this batch with CUDA events (best of the second
+    // and third run of each shape): first the LZ4 stage's CTA width (2, 4,
+    // 8 or 16 chunks per CTA) with the wavelet kernel's default variant,
+    // then the wavelet kernel's row-prefetch variant with that width. Every
+    // shape writes the same bytes.
     cz_stream tmp;
-    if (tune && q.encoder == CZ_ENCODER_LZ4) {
-        const int cand[3] = {2, 4, 8};
+    if (tune) {
         pl->c->timing = true;
-        float best = 1e30f;
-        for (int k = 0; k < 3; ++k) {
-            pl->job.lz_warps = cand[k];
+        auto time_stage = [&](int stage, float &best_t) -> int {
             float t = 1e30f;
             for (int rep = 0; rep < 3; ++rep) {
-                if ((rc = enqueue(pl->c, pl->job, pl->st, true)) != CZ_OK) return bail(rc, "tune");
-                if ((rc = finish(pl->c, pl->job, pl->st, &tmp)) != CZ_OK) return bail(rc, "tune");
+                int r = enqueue(pl->c, pl->job, pl->st, true);
+                if (r == CZ_OK) r = finish(pl->c, pl->job, pl->st, &tmp);
+                if (r != CZ_OK) return r;
                 collect(pl->c);
-                if (rep > 0) t = std::min(t, pl->c->stage_ms[1]);
+                if (rep > 0) t = std::min(t, pl->c->stage_ms[stage]);
             }
-            pl->tune_ms[k] = t;
-            if (t < best) {
-                best = t;
+            best_t = t;
+            return CZ_OK;
+        };
+        if (q.encoder == CZ_ENCODER_LZ4) {
+            const int cand[4] = {2, 4, 8, 16};
+            int pick = 4;
+            float best = 1e30f;
+            for (int k = 0; k < 4; ++k) {
                 pl->job.lz_warps = cand[k];
+                if ((rc = time_stage(1, pl->lz_ms[k])) != CZ_OK) return bail(rc, "tune");
+                if (pl->lz_ms[k] < best) {
+                    best = pl->lz_ms[k];
+                    pick = cand[k];
+                }
             }
+            pl->job.lz_warps = pick;
         }
-        // restore the winner (the loop leaves the last candidate set)
-        for (int k = 0; k < 3; ++k)
-            if (pl->tune_ms[k] == best) pl->job.lz_warps = cand[k];
+        int vpick = 0;
+        for (int v = 0; v < 2; ++v) {
+            pl->job.enc_variant = v;
+            if ((rc = time_stage(0, pl->enc_ms[v])) != CZ_OK) return bail(rc, "tune");
+            if (pl->enc_ms[v] < pl->enc_ms[vpick]) vpick = v;
+        }
+        pl->job.enc_variant = vpick;
         pl->c->timing = false;
     }
     // one graph: memsets, wavelet kernel, chunk setup, scans, LZ4, gather
@@ -835,7 +854,21 @@ int cz_plan_info(const cz_plan *pl, int *lz_warps, float *tune_ms)
     if (!pl) return CZ_E_ARG;
     if (lz_warps) *lz_warps = pl->job.lz_warps;
     if (tune_ms)
-        for (int k = 0; k < 3; ++k) tune_ms[k] = pl->tune_ms[k];
+        for (int k = 0; k < 3; ++k) tune_ms[k] = pl->lz_ms[k];
+    return CZ_OK;
+}
+
+int cz_plan_shape(const cz_plan *pl, int *shape, float *ms)
+{
+    if (!pl) return CZ_E_ARG;
+    if (shape) {
+        shape[0] = pl->job.lz_warps;
+        shape[1] = pl->job.enc_variant;
+    }
+    if (ms) {
+        for (int k = 0; k < 4; ++k) ms[k] = pl->lz_ms[k];
+        for (int v = 0; v < 2; ++v) ms[4 + v] = pl->enc_ms[v];
+    }
     return CZ_OK;
 }
 

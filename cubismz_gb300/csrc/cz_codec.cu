@@ -32,7 +32,10 @@
 
 namespace cz {
 
-template <int KIND>
+// SPLIT: the next block's rows are loaded by the warps level 16 leaves idle
+// during level 16 and by the others after it; otherwise every thread loads
+// its rows after level 32 (one of the autotuner's shapes).
+template <int KIND, bool SPLIT>
 __device__ __forceinline__ void encode_body(const CzField *fields, int nfields, long long total_blocks, int zerobits,
                                             int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue)
 {
@@ -88,7 +91,7 @@ __device__ __forceinline__ void encode_body(const CzField *fields, int nfields, 
         // the next block's rows load while this one finishes: the warps
         // that level 16 leaves idle (threads >= 256) now, the others once
         // level 16 is done
-        if (threadIdx.x >= 256 && gn < total_blocks) load_rows(locate(fields, nfields, gn), pf);
+        if ((!SPLIT || threadIdx.x >= 256) && gn < total_blocks) load_rows(locate(fields, nfields, gn), pf);
         // ---- level 16 (z, x, y) on the [0,16)^3 corner
         sweep<16, 2, true, KIND>(s.sb);
         __syncthreads();
@@ -104,7 +107,7 @@ __device__ __forceinline__ void encode_body(const CzField *fields, int nfields, 
             emit16(s, x, z, keep_bits<16>(v, eps));
         }
         __syncthreads();
-        if (threadIdx.x < 256 && gn < total_blocks) load_rows(locate(fields, nfields, gn), pf);
+        if (SPLIT && threadIdx.x < 256 && gn < total_blocks) load_rows(locate(fields, nfields, gn), pf);
         // ---- level 8 (y, z, x) on the [0,8)^3 corner
         sweep<8, 1, true, KIND>(s.sb);
         __syncthreads();
@@ -126,12 +129,12 @@ __device__ __forceinline__ void encode_body(const CzField *fields, int nfields, 
 }
 
 // One CTA per SM with the whole register file.
-template <int KIND>
+template <int KIND, bool SPLIT>
 __global__ void __launch_bounds__(kNT, 1)
 encode_kernel(const CzField *fields, int nfields, long long total_blocks, int zerobits, int shuffle,
               uint8_t *stage, int *rec_bytes, unsigned long long *queue)
 {
-    encode_body<KIND>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
+    encode_body<KIND, SPLIT>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
 }
 
 // Error statistics of a decoded block against a reference field (the
@@ -367,9 +370,9 @@ extern "C" int cz_codec_smem_bytes(void) { return kSmBytes; }
 template <int KIND>
 static cudaError_t launch_encode(const CzField *fields, int nfields, long long total_blocks, int zerobits,
                                  int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
-                                 cudaStream_t st)
+                                 cudaStream_t st, int variant)
 {
-    auto k = encode_kernel<KIND>;
+    auto k = variant == 1 ? encode_kernel<KIND, false> : encode_kernel<KIND, true>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
     if (e != cudaSuccess) return e;
     k<<<grid, kNT, kSmBytes, st>>>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue);
@@ -392,15 +395,18 @@ static cudaError_t launch_decode(const CzField *fields, int nfields, long long t
 
 cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long long total_blocks, int zerobits,
                              int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
-                             cudaStream_t st)
+                             cudaStream_t st, int variant)
 {
     switch (wkind(wtype)) {
     case 1:
-        return launch_encode<1>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
+        return launch_encode<1>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
+                                variant);
     case 2:
-        return launch_encode<2>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
+        return launch_encode<2>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
+                                variant);
     default:
-        return launch_encode<3>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st);
+        return launch_encode<3>(fields, nfields, total_blocks, zerobits, shuffle, stage, rec_bytes, queue, grid, st,
+                                variant);
     }
 }
 

@@ -16,9 +16,11 @@ struct CzField {
 
 extern "C" int cz_codec_smem_bytes(void);
 
+// variant 0: the next block's rows load in two halves, by the warps each
+// level leaves idle; 1: all at once after level 32 (same records)
 cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long long total_blocks, int zerobits,
                              int shuffle, uint8_t *stage, int *rec_bytes, unsigned long long *queue, int grid,
-                             cudaStream_t st);
+                             cudaStream_t st, int variant = 0);
 // Record of block g at base + rec_off[g] ([int32 nbytes][record]); a
 // negative rec_off marks a block whose record is missing (status -1).
 // diff_ref (optional, a field of the same geometry as fields[0]): per-block
@@ -48,8 +50,8 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 // bytes past its end (buffers carry tail room). Outputs may start anywhere.
 // records != 0: chunks hold block records with shuffled byte planes; the
 // search skips planes 1 and 2 (copied as literals).
-// warps: 2, 4, 8 or 32 warps (chunks) per CTA (32 fills an SM); any choice
-// gives the same bytes.
+// warps: 2, 4, 8, 16 or 32 warps (chunks) per CTA (32 fills an SM); any
+// choice gives the same bytes.
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
                                  int grid, cudaStream_t st);

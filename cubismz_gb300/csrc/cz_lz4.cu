@@ -910,6 +910,7 @@ cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, con
     switch (warps) {
     case 2: return launch_enc<2, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
     case 8: return launch_enc<8, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
+    case 16: return launch_enc<16, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
     case 32: return launch_enc<32, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
     default: return launch_enc<4, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
     }

@@ -220,8 +220,9 @@ int cz_refit(cz_ctx *ctx, const float *d_field, int nx, int ny, int nz, const cz
 /* ---- batch plans (device buffers) -------------------------------------- */
 /* A batch of fields fixed once (device pointers, extents, thresholds) and
  * compressed many times: cz_plan_create sizes a private set of buffers,
- * optionally tunes the launch shape of the LZ4 stage on the batch itself
- * (tune != 0: 2, 4 or 8 chunks per CTA, timed with CUDA events; all give
+ * optionally tunes the launch shape on the batch itself (tune != 0, timed
+ * with CUDA events: the LZ4 stage's CTA width, 2, 4, 8 or 16 chunks per
+ * CTA, then the wavelet kernel's row-prefetch variant; every shape writes
  * the same bytes), and captures the whole pipeline (one persistent wavelet
  * launch over every field's blocks through the device work queue, chunk
  * setup, scans, LZ4, gather) in a CUDA graph. cz_plan_launch is one graph
@@ -236,6 +237,12 @@ int cz_plan_create(cz_ctx *ctx, int nfields, const float *const *d_fields, const
 int cz_plan_launch(cz_plan *plan, void *stream);
 int cz_plan_result(cz_plan *plan, void *stream, cz_stream *all, cz_stream *per_field);
 int cz_plan_info(const cz_plan *plan, int *lz_warps, float *tune_ms /* 3: LZ4 ms at 2, 4, 8 */);
+/* The tuned shape: shape[0] = LZ4 chunks per CTA, shape[1] = wavelet kernel
+ * variant (0: the next block's rows load in two halves by the warps each
+ * level leaves idle, 1: all at once after level 32); ms[0..3] = LZ4 stage at
+ * 2, 4, 8, 16 chunks per CTA, ms[4..5] = wavelet kernel in variant 0, 1
+ * (-1 where not timed). No counterpart in the reference. */
+int cz_plan_shape(const cz_plan *plan, int *shape /* 2 */, float *ms /* 6 */);
 const char *cz_plan_last_error(const cz_plan *plan);
 int cz_plan_destroy(cz_plan *plan);
 

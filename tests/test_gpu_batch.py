@@ -27,7 +27,15 @@ def test_plan_graph_batch(cz):
     dev = [torch.from_numpy(f).cuda() for f in fields]
     plan = cz.Plan(dev, eps, wtype=1, zerobits=4, shuffle=True, encoder="lz4", tune=True)
     info = plan.info()
-    assert info["lz4_warps_per_cta"] in (2, 4, 8) and all(t > 0 for t in info["tune_ms"].values())
+    assert info["lz4_warps_per_cta"] in (2, 4, 8, 16) and all(t > 0 for t in info["tune_ms"].values())
+    # the tuned shape: the fastest LZ4 width and wavelet-kernel variant timed
+    assert info["shape"]["lz4_chunks_per_cta"] == info["lz4_warps_per_cta"]
+    assert all(t > 0 for t in info["lz4_stage_ms"].values())
+    assert all(t > 0 for t in info["wavelet_kernel_ms"].values())
+    lz = info["lz4_stage_ms"]
+    assert lz[info["lz4_warps_per_cta"]] == min(lz.values())
+    wk = info["wavelet_kernel_ms"]
+    assert wk[("split_prefetch", "joint_prefetch")[info["shape"]["wavelet_variant"]]] == min(wk.values())
 
     def check(fs):
         for _ in range(2):
