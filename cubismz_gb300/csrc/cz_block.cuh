@@ -319,13 +319,18 @@ __device__ __forceinline__ void load_survivors(const Shared &s, int S, Get &&get
         const int o = r < kSegs ? s.off[r] : S;
         const int first = __shfl_sync(0xffffffffu, o, 0);
         const int total = __shfl_sync(0xffffffffu, o + __popc(m), 31) - first;
-        if (total == 0) continue;
-        for (int b = lane; b < total; b += 32) stg[b] = get(first + b);
-        __syncwarp();
+        if (total > 0) {
+            for (int b = lane; b < total; b += 32) stg[b] = get(first + b);
+            __syncwarp();
+        }
         int base = 0, stride = 0;
         if (r < kSegs) run_geom(r, base, stride);
         int i = o - first;
-        for (unsigned mm = m; mm; mm &= mm - 1) s.sb[base + (__ffs(mm) - 1) * stride] = stg[i++];
+        // every place of the run: its survivor or zero (the runs and the
+        // coarse corner cover the whole block, so no separate zeroing)
+        const int len = r < kSegBase16 ? 4 : (r < kSegBase32 ? 8 : 16);
+        if (r < kSegs)
+            for (int e = 0; e < len; ++e) s.sb[base + e * stride] = ((m >> e) & 1u) ? stg[i++] : 0.f;
         __syncwarp();
     }
 }

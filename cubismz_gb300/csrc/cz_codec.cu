@@ -240,16 +240,18 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
         if (nel - expected == 1) nel--;  // :247-250
         const bool ok = size_ok && nel == expected && !s_bad;
         if (threadIdx.x == 0) status[g] = ok ? 0 : -1;
-        // ---- load (FullWaveletTransform.h:99-150): zeros, then every survivor
-        // at its place, read in stream order (consecutive across each warp)
-        for (int i = threadIdx.x; i < kBS3; i += kNT) s.sb[pidx(i & 31, (i >> 5) & 31, i >> 10)] = 0.f;
-        __syncthreads();
+        // ---- load (FullWaveletTransform.h:99-150): every survivor at its
+        // place, read in stream order (consecutive across each warp), and
+        // zeros at every other place (the runs cover the block); a bad
+        // record leaves the block all zeros
         if (ok) {
             Payload pl;
             pl.p = slot + 4 + kMaskBytes;
             pl.c = payload / 4;
             pl.shuffle = shuffle != 0;
             load_survivors(s, expected, [&](int k) { return pl.get(k); });
+        } else {
+            for (int i = threadIdx.x; i < kBS3; i += kNT) s.sb[pidx(i & 31, (i >> 5) & 31, i >> 10)] = 0.f;
         }
         __syncthreads();
         // ---- iwt: level 8 (x, z, y), level 16 (y, x, z), level 32 (z, y, x)
