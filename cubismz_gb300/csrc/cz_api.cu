@@ -50,7 +50,7 @@ struct cz_ctx {
     std::string err;
     DevBuf fields, stage, rec_bytes, chunk_in, in_off, in_len, blk_dst, lz_off, lz_out, lz_len, out_off, out_data,
         queue, status, flag, rec_off, dec, dec_off, dec_cap, dec_len, raw_off, chunk_rec, block_chunk, block_subid,
-        tmp_field, tmp_in, refit, diff, zout, zoff, zlen, ierr;
+        tmp_field, tmp_in, refit, diff, zout, zoff, zlen, ierr, lz_hole;
     void *pin = nullptr;  // small pinned host scratch
     size_t pin_cap = 0;
     // geometry of the last compressed stream
@@ -226,6 +226,7 @@ int prepare(cz_ctx *c, const std::vector<CzField> &fields, long long nblocks, co
         CZ_TRY(grow(c, c->chunk_in, (size_t)nchunks * bpc * kSlotBytes));
     }
     if (p->encoder != CZ_ENCODER_NONE) CZ_TRY(grow(c, c->lz_out, (size_t)nchunks * job.lz_slot));
+    if (p->encoder == CZ_ENCODER_LZ4) CZ_TRY(grow(c, c->lz_hole, sizeof(int4) * (size_t)nchunks));
     if (zlib) {
         CZ_TRY(grow(c, c->zout, (size_t)nchunks * job.z_slot));
         CZ_TRY(grow(c, c->zoff, sizeof(long long) * nchunks));
@@ -278,9 +279,10 @@ int enqueue(cz_ctx *c, const Job &job, cudaStream_t st, bool marks)
     if (p->encoder == CZ_ENCODER_LZ4) {
         const int per = job.lz_warps;
         const int lzgrid = std::max(1, std::min((nchunks + per - 1) / per, c->sms * (32 / per)));
+        // the records' incompressible planes are left to the gather (hole)
         CZ_CUDA(c, cz_launch_lz4_encode(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
                                         P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<int>(c->lz_len),
-                                        p->shuffle ? 1 : 0, per, lzgrid, st));
+                                        p->shuffle ? 1 : 0, per, lzgrid, st, P<int4>(c->lz_hole)));
         CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len), nchunks, P<int>(c->flag), st));
         gsrc = P<uint8_t>(c->lz_out);
         gsrc_off = P<long long>(c->lz_off);
@@ -302,7 +304,9 @@ int enqueue(cz_ctx *c, const Job &job, cudaStream_t st, bool marks)
     }
     if (marks) CZ_TRY(mark(c, 2, st));
     CZ_CUDA(c, cz_launch_scan(glen, nchunks, P<long long>(c->out_off), st));
-    CZ_CUDA(c, cz_launch_gather(gsrc, gsrc_off, glen, nchunks, P<uint8_t>(c->out_data), P<long long>(c->out_off), st));
+    const bool holes = p->encoder == CZ_ENCODER_LZ4;
+    CZ_CUDA(c, cz_launch_gather(gsrc, gsrc_off, glen, nchunks, P<uint8_t>(c->out_data), P<long long>(c->out_off), st,
+                                holes ? P<int4>(c->lz_hole) : nullptr, chunk_src, P<long long>(c->in_off)));
     if (marks) CZ_TRY(mark(c, 3, st));
     return CZ_OK;
 }
@@ -460,7 +464,7 @@ int cz_destroy(cz_ctx *c)
                      &c->blk_dst, &c->lz_off,  &c->lz_out,    &c->lz_len,    &c->out_off,     &c->out_data,
                      &c->queue,   &c->status,  &c->flag,      &c->rec_off,   &c->dec,         &c->dec_off,
                      &c->dec_cap, &c->dec_len, &c->raw_off,   &c->chunk_rec, &c->block_chunk, &c->block_subid,
-                     &c->tmp_field, &c->tmp_in};
+                     &c->tmp_field, &c->tmp_in, &c->lz_hole};
     for (DevBuf *b : all)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->ev)
@@ -1215,7 +1219,8 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
             // the next slabs then share the GPU SM by SM
             const int lzgrid = std::max(1, std::min((n + 31) / 32, c->sms));
             CZ_CUDA(c, cz_launch_lz4_encode(stage, src_off, len, n, lzo, P<long long>(c->lz_off) + f0,
-                                            P<int>(c->lz_len) + f0, p->shuffle ? 1 : 0, 32, lzgrid, ls));
+                                            P<int>(c->lz_len) + f0, p->shuffle ? 1 : 0, 32, lzgrid, ls,
+                                            P<int4>(c->lz_hole) + f0));
             CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len) + f0, n, P<int>(c->flag), ls));
             CZ_CUDA(c, cudaEventRecord(c->ev_lz[i], ls));
             src = lzo;
@@ -1225,7 +1230,8 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
         }
         CZ_CUDA(c, cudaStreamWaitEvent(c->s_gather, ready, 0));
         CZ_CUDA(c, cz_launch_scan_from(len, n, P<long long>(c->out_off) + f0, c->s_gather));
-        CZ_CUDA(c, cz_launch_gather(src, src_off, len, n, dst, P<long long>(c->out_off) + f0, c->s_gather));
+        CZ_CUDA(c, cz_launch_gather(src, src_off, len, n, dst, P<long long>(c->out_off) + f0, c->s_gather,
+                                    lz4 ? P<int4>(c->lz_hole) + f0 : nullptr, stage, P<long long>(c->in_off) + f0));
     }
     CZ_CUDA(c, cudaEventRecord(c->ev_join, c->s_gather));
     CZ_CUDA(c, cudaStreamWaitEvent(st, c->ev_join, 0));

@@ -52,9 +52,13 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 // search skips planes 1 and 2 (copied as literals).
 // warps: 2, 4, 8, 16 or 32 warps (chunks) per CTA (32 fills an SM); any
 // choice gives the same bytes.
+// hole (optional): written for every chunk, {out position, input position,
+// length, 0} of one literal-only span (byte planes 1 and 2 of a record
+// chunk) that the encoder leaves unwritten in its output for the gather to
+// copy from the input; length 0 when there is none.
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
-                                 int grid, cudaStream_t st);
+                                 int grid, cudaStream_t st, int4 *hole = nullptr);
 // The LZ77 parse of the LZ4 encoder for DEFLATE: distances up to 32 KiB,
 // 8-byte sequence records (zl::seq_pack) per chunk at seq + seq_off[c]
 // (capacity 8 * (in_len/4 + 2) bytes); seq_bytes[c] = record bytes.
@@ -75,8 +79,11 @@ cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, con
                                  cudaStream_t st);
 
 // Stream assembly helpers (cz_lz4.cu, cz_stream.cu)
+// With hole (from cz_launch_lz4_encode): the span of each chunk that the
+// encoder left unwritten comes from hsrc + hsrc_off[c] + hole[c].y.
 cudaError_t cz_launch_gather(const uint8_t *src, const long long *src_off, const int *len, int nchunks,
-                             uint8_t *dst, const long long *dst_off, cudaStream_t st);
+                             uint8_t *dst, const long long *dst_off, cudaStream_t st, const int4 *hole = nullptr,
+                             const uint8_t *hsrc = nullptr, const long long *hsrc_off = nullptr);
 // Chunk layout of the encode side: chunk c holds blocks [c*bpc, (c+1)*bpc).
 // Fills in_off/in_len (chunk inputs in chunk_in, or in the slots when bpc=1),
 // blk_dst (where block g's [nbytes][record] goes inside chunk_in) and lz_off.

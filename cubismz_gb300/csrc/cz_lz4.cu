@@ -20,8 +20,11 @@
 // reference's acceleration idea, lz4.c:389-393). Chunks of block records
 // ([int32 nbytes][mask][4 byte planes], shuffle on) skip the search over
 // byte planes 1 and 2 -- the two middle mantissa bytes, which do not
-// compress -- and copy them as literals. The same parse in SEQ mode feeds
-// the DEFLATE encoder (cz_zlib.cu).
+// compress -- and copy them as literals; those literal bytes are not even
+// copied here: the encoder leaves their span of its output unwritten and
+// records it per chunk, and the gather that packs the stream copies them
+// straight from the records. The same parse in SEQ mode feeds the DEFLATE
+// encoder (cz_zlib.cu).
 // Decoder: the same acceptance tests and error convention as
 // LZ4_uncompress_unknownOutputSize (-(input position) on malformed input; an
 // empty input yields 0). Windows of 128 input bytes are parsed
@@ -164,6 +167,7 @@ __device__ __forceinline__ void next_skip(Skip &k, const uint8_t *src, int L)
 //             every lane writes its own; literal runs longer than 32 bytes
 //             are queued and copied by the whole warp.
 constexpr int kSW = 512, kSub = kSW / 32, kMaxSeqLane = kSub / 4;
+constexpr int kMinHole = 256;  // smallest literal-only span left to the gather
 // Hash table entry: position modulo 2^18 in the high bits, a 14-bit tag of
 // the 4-byte sequence in the low bits. A tag hit is only a candidate: the
 // walk measures the match from its first byte and drops it below 4 bytes.
@@ -230,7 +234,7 @@ struct LzEncWarp {
 template <int kLzWarps, bool SEQ>
 __global__ void __launch_bounds__(kLzWarps * 32)
 lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
-                  uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records)
+                  uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records, int4 *hole)
 {
     constexpr int kMaxOff = SEQ ? zl::kMaxDist : 65535;
     // up to 8 warps in static shared memory; 32 (a whole SM) in dynamic
@@ -255,6 +259,11 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
         __syncwarp();
         int pos = 0, anchor = 0, op = 0, miss = 0;
         bool overflow = false;
+        // the literal-only planes last jumped over, and whether the chunk's
+        // one deferred copy (left to the gather) is taken
+        int hlo = 0, hhi = 0;
+        bool deferred = hole == nullptr || !records;
+        if (hole && lane == 0) hole[c] = make_int4(0, 0, 0, 0);  // written for every chunk
         Skip sk;
         sk.on = records != 0;
         sk.next = 0;
@@ -264,6 +273,8 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
         while (L >= kMfLimit + 1 && pos <= mflimit && !overflow) {
             if (pos >= sk.lo) {  // literal-only planes: jump over them
                 if (pos < sk.hi) pos = sk.hi;
+                hlo = sk.lo;
+                hhi = sk.hi;
                 next_skip(sk, src, L);
                 miss = 0;
                 continue;
@@ -445,7 +456,17 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             }
             for (int i = 0; i < nl; ++i) {
                 const int4 t = longq[i];
-                warp_copy(dst + t.x, src + t.y, t.z, lane);
+                // the planes inside this run go to the gather (once per
+                // chunk): it copies them from the records into the stream
+                const int a = max(t.y, hlo), b = min(t.y + t.z, hhi);
+                if (!deferred && b - a >= kMinHole) {
+                    warp_copy(dst + t.x, src + t.y, a - t.y, lane);
+                    warp_copy(dst + t.x + (b - t.y), src + b, t.y + t.z - b, lane);
+                    if (lane == 0) hole[c] = make_int4(t.x + (a - t.y), a, b - a, 0);
+                    deferred = true;
+                } else {
+                    warp_copy(dst + t.x, src + t.y, t.z, lane);
+                }
             }
             __syncwarp();
             op += total;
@@ -470,7 +491,15 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     if (lit >= 15) put_len_serial(dst + op + 1, lit - 15);
                 }
                 op += 1 + (lit >= 15 ? len_bytes(lit - 15) : 0);
-                warp_copy(dst + op, src + anchor, lit, lane);
+                const int a = max(anchor, hlo), b = min(L, hhi);
+                if (!deferred && b - a >= kMinHole) {  // the planes to the gather, as above
+                    warp_copy(dst + op, src + anchor, a - anchor, lane);
+                    warp_copy(dst + op + (b - anchor), src + b, L - b, lane);
+                    if (lane == 0) hole[c] = make_int4(op + (a - anchor), a, b - a, 0);
+                    deferred = true;
+                } else {
+                    warp_copy(dst + op, src + anchor, lit, lane);
+                }
                 op += lit;
             }
         }
@@ -842,18 +871,13 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
     }
 }
 
-// One CTA per chunk: bytes until the destination is 16-byte aligned, then
+// n bytes from s to d by the CTA: bytes until d is 16-byte aligned, then
 // 16-byte stores (each built from five 4-byte loads with funnel shifts), then
 // the tail. Wide stores matter when the destination is host memory written
-// over the CPU-GPU link.
-__global__ void gather_kernel(const uint8_t *__restrict__ src, const long long *src_off, const int *len,
-                              uint8_t *__restrict__ dst, const long long *dst_off)
+// over the CPU-GPU link. Reads up to 4 bytes past s + n.
+__device__ __forceinline__ void cta_copy(uint8_t *__restrict__ d, const uint8_t *__restrict__ s, int n)
 {
-    const int c = blockIdx.x;
-    const int n = len[c];
     if (n <= 0) return;
-    const uint8_t *s = src + src_off[c];
-    uint8_t *d = dst + dst_off[c];
     int h = (int)((16 - (reinterpret_cast<uintptr_t>(d) & 15)) & 15);
     if (h > n) h = n;
     if ((int)threadIdx.x < h) d[threadIdx.x] = s[threadIdx.x];
@@ -880,6 +904,29 @@ __global__ void gather_kernel(const uint8_t *__restrict__ src, const long long *
     if ((int)threadIdx.x < t) d[h + 16 * nwd + threadIdx.x] = s2[16 * nwd + threadIdx.x];
 }
 
+// One CTA per chunk: the chunk's bytes to dst + dst_off[c]. With `hole`
+// (LZ4 of block records), bytes [hole.x, hole.x + hole.z) of the chunk's
+// output are the input bytes at hsrc + hsrc_off[c] + hole.y, which the
+// encoder left unwritten.
+__global__ void gather_kernel(const uint8_t *__restrict__ src, const long long *src_off, const int *len,
+                              uint8_t *__restrict__ dst, const long long *dst_off, const int4 *hole,
+                              const uint8_t *__restrict__ hsrc, const long long *hsrc_off)
+{
+    const int c = blockIdx.x;
+    const int n = len[c];
+    if (n <= 0) return;
+    const uint8_t *s = src + src_off[c];
+    uint8_t *d = dst + dst_off[c];
+    const int4 hl = hole ? hole[c] : make_int4(0, 0, 0, 0);
+    if (hl.z > 0) {
+        cta_copy(d, s, hl.x);
+        cta_copy(d + hl.x, hsrc + hsrc_off[c] + hl.y, hl.z);
+        cta_copy(d + hl.x + hl.z, s + hl.x + hl.z, n - hl.x - hl.z);
+    } else {
+        cta_copy(d, s, n);
+    }
+}
+
 }  // namespace cz
 
 using namespace cz;
@@ -890,7 +937,7 @@ using namespace cz;
 template <int W, bool SEQ>
 static cudaError_t launch_enc(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                               uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
-                              cudaStream_t st)
+                              cudaStream_t st, int4 *hole = nullptr)
 {
     const int sm = W <= 8 ? 0 : (int)sizeof(LzEncWarp) * W;
     auto k = lz4_encode_kernel<W, SEQ>;
@@ -898,21 +945,23 @@ static cudaError_t launch_enc(const uint8_t *in, const long long *in_off, const 
         const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         if (e != cudaSuccess) return e;
     }
-    k<<<grid, W * 32, sm, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records);
+    k<<<grid, W * 32, sm, st>>>(in, in_off, in_len, nchunks, out, out_off, out_len, records, hole);
     return cudaGetLastError();
 }
 
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
-                                 int grid, cudaStream_t st)
+                                 int grid, cudaStream_t st, int4 *hole)
 {
     if (nchunks <= 0) return cudaSuccess;
     switch (warps) {
-    case 2: return launch_enc<2, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
-    case 8: return launch_enc<8, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
-    case 16: return launch_enc<16, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
-    case 32: return launch_enc<32, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
-    default: return launch_enc<4, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st);
+    case 2: return launch_enc<2, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+    case 8: return launch_enc<8, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+    case 16:
+        return launch_enc<16, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+    case 32:
+        return launch_enc<32, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+    default: return launch_enc<4, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
     }
 }
 
@@ -934,9 +983,10 @@ cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, con
 }
 
 cudaError_t cz_launch_gather(const uint8_t *src, const long long *src_off, const int *len, int nchunks,
-                             uint8_t *dst, const long long *dst_off, cudaStream_t st)
+                             uint8_t *dst, const long long *dst_off, cudaStream_t st, const int4 *hole,
+                             const uint8_t *hsrc, const long long *hsrc_off)
 {
     if (nchunks <= 0) return cudaSuccess;
-    gather_kernel<<<nchunks, 256, 0, st>>>(src, src_off, len, dst, dst_off);
+    gather_kernel<<<nchunks, 256, 0, st>>>(src, src_off, len, dst, dst_off, hole, hsrc, hsrc_off);
     return cudaGetLastError();
 }
