@@ -578,6 +578,14 @@ def run_ours(args, rank, world, local_rank):
     d1.record(stream)
     torch.cuda.synchronize()
     dms = d0.elapsed_time(d1) / args.steps
+    # decompress stage times: [0] LZ4 decode, [1] record location, [2] decode kernel
+    ctx.set_timing(True)
+    dst_ms = []
+    for _ in range(max(3, min(args.steps, 10))):
+        cz.decompress_field(data, off, field.shape, WTYPE, SHUFFLE, encoder="lz4", out=out)
+        dst_ms.append(ctx.stage_times())
+    ctx.set_timing(False)
+    dst_ms = np.mean(np.array(dst_ms), axis=0)
     dec = out.cpu().numpy()
     err = np.abs(dec.astype(np.float64) - field)
     mse = float((err * err).mean())
@@ -637,6 +645,9 @@ def run_ours(args, rank, world, local_rank):
                 "traffic": t, "algorithmic_bytes": alg, "ms": ms, "peak_source": peak_kind}
 
     roof_enc = roof("encode_kernel", nbytes + raw_bytes, enc)  # field read + records written
+    # decompress: LZ4 chunks read + records written; records read + field written
+    roof_lzd = roof("lz4_decode_kernel", comp_bytes + raw_bytes, float(dst_ms[0]))
+    roof_dec = roof("decode_kernel", raw_bytes + nbytes, float(dst_ms[2]))
     roof_lz = roof("lz4_encode_kernel", raw_bytes + comp_bytes, lz)  # records read + chunks written
     dominant = roof_lz if lz > enc else roof_enc
     # ---- CPU baseline (oracle port, all host cores, same field)
@@ -655,12 +666,15 @@ def run_ours(args, rank, world, local_rank):
                         "pre_lz4_bytes": raw_bytes, "psnr_db": psnr, "max_abs_err": float(err.max())},
         "stages_ms": {"encode_kernel": enc, "lz4": float(np.mean(lz_ms)), "assembly": float(np.mean(asm_ms))},
         "decompress": {"value": world * nbytes / (dms * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": dms,
+                       "stages_ms": {"lz4_decode": float(dst_ms[0]), "locate": float(dst_ms[1]),
+                                     "decode_kernel": float(dst_ms[2])},
+                       "roofline_frac": (comp_bytes + nbytes) / (dms * 1e-3) / 1e9 / peaks()[0],
                        "cpu_baseline": {"value": nbytes / cpu_ds / 1e9, "unit": "GB/s", "cores": threads,
                                         "kind": "port", "sample": dsample}},
         "e2e": {"value": world * nbytes / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": image_bytes},
         "roofline": dominant,
-        "roofline_kernels": [roof_enc, roof_lz],
+        "roofline_kernels": [roof_enc, roof_lz, roof_lzd, roof_dec],
         "cpu_baseline": {"value": nbytes / cpu_s / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": sample, "gbs_by_threads": cpu_thread_counts(field, eps),
                          "by_threads_sample": f"first 64 z-planes of the {SIZE}^3 field (512 blocks)"},

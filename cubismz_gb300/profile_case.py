@@ -5,9 +5,10 @@ stage (LZ4 by default, or zlib), then decompressed twice. Prints the
 per-stage device times of each call. With --ingest, the same field goes
 through the HDF5 tools' layout instead: to z-fastest and back, three times
 each (the tile transpose kernels). --shape nz,ny,nx picks another field
-size (multiples of 32), e.g. 512,512,512 for the bench's occupancy.
+size (multiples of 32), e.g. 512,512,512 for the bench's occupancy;
+--bench-field takes the bench's own 512^3 field.
 
-    python -m cubismz_gb300.profile_case [--encoder lz4|zlib] [--ingest] [--shape nz,ny,nx]
+    python -m cubismz_gb300.profile_case [--encoder lz4|zlib] [--ingest] [--shape nz,ny,nx] [--bench-field]
 """
 import argparse
 
@@ -19,13 +20,19 @@ def main():
     ap.add_argument("--encoder", default="lz4", choices=["lz4", "zlib"])
     ap.add_argument("--ingest", action="store_true")
     ap.add_argument("--shape", default="256,512,512")
+    ap.add_argument("--bench-field", action="store_true",
+                    help="the bench's 512^3 field (200 blobs, 12 interfaces, seed 0) instead")
     args = ap.parse_args()
     enc = args.encoder
     import torch
     import cubismz_gb300 as cz
     from cubismz_gb300 import synth
     shape = tuple(int(x) for x in args.shape.split(","))
-    field = synth.generate(shape, seed=3, blobs=60, interfaces=6)
+    if args.bench_field:
+        field = synth.config_field("large", 0)
+        shape = field.shape
+    else:
+        field = synth.generate(shape, seed=3, blobs=60, interfaces=6)
     eps = float(np.float32(1e-3 * (field.max() - field.min())))
     f = torch.from_numpy(field).cuda()
     if args.ingest:
