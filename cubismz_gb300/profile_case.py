@@ -6,9 +6,11 @@ per-stage device times of each call. With --ingest, the same field goes
 through the HDF5 tools' layout instead: to z-fastest and back, three times
 each (the tile transpose kernels). --shape nz,ny,nx picks another field
 size (multiples of 32), e.g. 512,512,512 for the bench's occupancy;
---bench-field takes the bench's own 512^3 field.
+--bench-field takes the bench's own 512^3 field. --refit runs the CGLS refit
+path twice instead, on the 256^3 refit field (60 blobs, 6 interfaces, seed
+0; absolute threshold 1e-3, 10 steps, wtype 1, zerobits 4, shuffle, LZ4).
 
-    python -m cubismz_gb300.profile_case [--encoder lz4|zlib] [--ingest] [--shape nz,ny,nx] [--bench-field]
+    python -m cubismz_gb300.profile_case [--encoder lz4|zlib] [--ingest] [--refit] [--shape nz,ny,nx] [--bench-field]
 """
 import argparse
 
@@ -19,6 +21,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--encoder", default="lz4", choices=["lz4", "zlib"])
     ap.add_argument("--ingest", action="store_true")
+    ap.add_argument("--refit", action="store_true")
     ap.add_argument("--shape", default="256,512,512")
     ap.add_argument("--bench-field", action="store_true",
                     help="the bench's 512^3 field (200 blobs, 12 interfaces, seed 0) instead")
@@ -28,6 +31,13 @@ def main():
     import cubismz_gb300 as cz
     from cubismz_gb300 import synth
     shape = tuple(int(x) for x in args.shape.split(","))
+    if args.refit:
+        f = torch.from_numpy(synth.config_field("refit", 0)).cuda()
+        for _ in range(2):
+            cf = cz.refit_field(f, 1e-3, 10, 1, 4, True, encoder=enc)
+        torch.cuda.synchronize()
+        print("refit payload", cf.nbytes)
+        return
     if args.bench_field:
         field = synth.config_field("large", 0)
         shape = field.shape
