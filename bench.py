@@ -222,7 +222,8 @@ def cpu_port_decompress_time(field, eps, threads, max_seconds=20.0):
     """Decompression on the host cores: the reference has none in parallel,
     so this is a loop of our own over chunks (OpenMP in the oracle port:
     LZ4 decode + WaveletCompressor::decompress per block) on the same
-    field's LZ4 chunks. Returns (seconds per full field, sample)."""
+    field's LZ4 chunks. Returns (seconds per full field, sample, bytes of
+    those chunks: the reference LZ4's payload for the same records)."""
     from oracle import czoracle as O
     data, off = O.field_compress(field, eps, WTYPE, ZEROBITS, 1, 1, 1, threads)
     best, reps = float("inf"), 0
@@ -231,7 +232,8 @@ def cpu_port_decompress_time(field, eps, threads, max_seconds=20.0):
         O.field_decompress(data, off, field.shape, WTYPE, 1, 1, 1, threads)
         best = min(best, time.perf_counter() - t0)
         reps += 1
-    return best, f"full {SIZE}^3 field, best of {reps}; OpenMP loop over chunks (the reference has no parallel decompress)"
+    return (best, f"full {SIZE}^3 field, best of {reps}; OpenMP loop over chunks (the reference has no parallel decompress)",
+            int(off[-1]))
 
 
 def cpu_thread_counts(field, eps, counts=(1, 12)):
@@ -621,6 +623,23 @@ def run_ours(args, rank, world, local_rank):
 
     if rank != 0:
         return
+    # ---- the LZ4 encoder's parse effort levels (cz_set_lz4_effort): the
+    # same compress at 0, 1 (the default, timed above) and 2
+    efforts = {}
+    try:
+        for lvl in (0, 1, 2):
+            ctx.set_lz4_effort(lvl)
+            for _ in range(2):
+                compress()
+            ctx.set_timing(True)
+            lzs = []
+            for _ in range(5):
+                cfe = compress()
+                lzs.append(ctx.stage_times()[1])
+            ctx.set_timing(False)
+            efforts[str(lvl)] = {"payload_bytes": cfe.nbytes, "lz4_stage_ms": float(np.mean(lzs))}
+    finally:
+        ctx.set_lz4_effort(1)
     zl = zlib_report(cz, f_dev, eps, max(3, min(args.steps, 20)))
     zl["ratio"] = nbytes / zl["payload_bytes"]
     zl["size_vs_lz4"] = zl["payload_bytes"] / comp_bytes
@@ -653,7 +672,7 @@ def run_ours(args, rank, world, local_rank):
     # ---- CPU baseline (oracle port, all host cores, same field)
     threads = os.cpu_count() or 1
     cpu_s, sample = cpu_port_time(field, eps, threads)
-    cpu_ds, dsample = cpu_port_decompress_time(field, eps, threads)
+    cpu_ds, dsample, ref_payload = cpu_port_decompress_time(field, eps, threads)
     line = {
         "metric": METRIC, "value": world * nbytes / (ms * 1e-3) / 1e9, "unit": "GB/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -663,7 +682,10 @@ def run_ours(args, rank, world, local_rank):
                    "field_bytes": nbytes, "l2": "inputs larger than L2 (512 MiB field)",
                    "parallelism": f"replicas x{world}"},
         "compression": {"ratio": nbytes / image_bytes, "cz_bytes": image_bytes, "payload_bytes": comp_bytes,
-                        "pre_lz4_bytes": raw_bytes, "psnr_db": psnr, "max_abs_err": float(err.max())},
+                        "pre_lz4_bytes": raw_bytes, "psnr_db": psnr, "max_abs_err": float(err.max()),
+                        "reference_lz4_payload_bytes": ref_payload,
+                        "payload_vs_reference_lz4": comp_bytes / ref_payload,
+                        "lz4_effort": 1, "lz4_effort_levels": efforts},
         "stages_ms": {"encode_kernel": enc, "lz4": float(np.mean(lz_ms)), "assembly": float(np.mean(asm_ms))},
         "decompress": {"value": world * nbytes / (dms * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": dms,
                        "stages_ms": {"lz4_decode": float(dst_ms[0]), "locate": float(dst_ms[1]),

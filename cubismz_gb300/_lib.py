@@ -26,7 +26,7 @@ MAX_RECORD = MASK_BYTES + 4 * BLOCK_ELEMS
 
 # exported symbols, as declared in include/czgpu.h
 EXPORTS = [
-    "cz_create", "cz_destroy", "cz_last_error", "cz_set_timing", "cz_stage_times",
+    "cz_create", "cz_destroy", "cz_last_error", "cz_set_timing", "cz_stage_times", "cz_set_lz4_effort",
     "cz_block_compress", "cz_block_decompress",
     "cz_lz4_bound", "cz_lz4_compress", "cz_lz4_decompress",
     "cz_field_compress", "cz_stream_copy", "cz_field_decompress", "cz_batch_compress",
@@ -74,6 +74,7 @@ def load():
     L.cz_last_error.argtypes = [vp]
     L.cz_last_error.restype = C.c_char_p
     L.cz_set_timing.argtypes = [vp, C.c_int]
+    L.cz_set_lz4_effort.argtypes = [vp, C.c_int]
     L.cz_stage_times.argtypes = [vp, fp, C.c_int]
     L.cz_block_compress.argtypes = [vp, fp, C.c_float, C.c_int, C.c_int, C.c_int, u8p, ip]
     L.cz_block_decompress.argtypes = [vp, u8p, C.c_int, C.c_int, C.c_int, fp]

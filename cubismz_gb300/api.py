@@ -38,6 +38,11 @@ class Context:
     def set_timing(self, on=True):
         self.check(self.L.cz_set_timing(self.h, 1 if on else 0))
 
+    def set_lz4_effort(self, effort):
+        """Parse effort of the LZ4 encoder for later calls: 0 fastest, 1
+        (default) with backward match extension, 2 most matches."""
+        self.check(self.L.cz_set_lz4_effort(self.h, int(effort)))
+
     def stage_times(self):
         """Per-stage device times (ms) of the last field call."""
         out = (C.c_float * 3)()

@@ -58,6 +58,8 @@ struct cz_ctx {
     int nchunks = 0, bpc = 1;
     // stage timing
     bool timing = false;
+    // LZ4 / LZ77 parse effort (cz_set_lz4_effort)
+    int lz_effort = 1;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float stage_ms[3] = {0, 0, 0};
     // the pipelined host-buffer path: copy, LZ4 and gather streams, events per slab
@@ -282,7 +284,7 @@ int enqueue(cz_ctx *c, const Job &job, cudaStream_t st, bool marks)
         // the records' incompressible planes are left to the gather (hole)
         CZ_CUDA(c, cz_launch_lz4_encode(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
                                         P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<int>(c->lz_len),
-                                        p->shuffle ? 1 : 0, per, lzgrid, st, P<int4>(c->lz_hole)));
+                                        p->shuffle ? 1 : 0, per, lzgrid, st, P<int4>(c->lz_hole), c->lz_effort));
         CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len), nchunks, P<int>(c->flag), st));
         gsrc = P<uint8_t>(c->lz_out);
         gsrc_off = P<long long>(c->lz_off);
@@ -291,7 +293,7 @@ int enqueue(cz_ctx *c, const Job &job, cudaStream_t st, bool marks)
         const int pgrid = std::max(1, std::min((nchunks + 3) / 4, c->sms * 8));
         CZ_CUDA(c, cz_launch_lz77_parse(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), nchunks,
                                         P<uint8_t>(c->lz_out), P<long long>(c->lz_off), P<int>(c->lz_len),
-                                        p->shuffle ? 1 : 0, pgrid, st));
+                                        p->shuffle ? 1 : 0, pgrid, st, c->lz_effort));
         CZ_CUDA(c, cz_launch_deflate(chunk_src, P<long long>(c->in_off), P<int>(c->in_len), P<uint8_t>(c->lz_out),
                                      P<long long>(c->lz_off), P<int>(c->lz_len), nchunks, p->shuffle ? 1 : 0,
                                      P<uint8_t>(c->zout),
@@ -487,6 +489,13 @@ int cz_set_timing(cz_ctx *c, int on)
 {
     if (!c) return CZ_E_ARG;
     c->timing = on != 0;
+    return CZ_OK;
+}
+
+int cz_set_lz4_effort(cz_ctx *c, int effort)
+{
+    if (!c || effort < 0 || effort > 2) return fail(c, CZ_E_ARG, "LZ4 effort must be 0, 1 or 2");
+    c->lz_effort = effort;
     return CZ_OK;
 }
 
@@ -760,6 +769,7 @@ int cz_plan_create(cz_ctx *c, int nfields, const float *const *d_fields, const i
     };
     int rc = cz_create(c->device, &pl->c);
     if (rc != CZ_OK) return bail(rc, "plan context");
+    pl->c->lz_effort = c->lz_effort;
     if (cudaStreamCreateWithFlags(&pl->st, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         return bail(CZ_E_CUDA, "plan stream");
@@ -943,7 +953,8 @@ int cz_lz4_compress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int 
     long long *doff = reinterpret_cast<long long *>(d + meta);
     int *dlen = reinterpret_cast<int *>(d + meta + 16);
     int *dout_len = reinterpret_cast<int *>(d + meta + 20);
-    CZ_CUDA(c, cz_launch_lz4_encode(d, doff, dlen, 1, dout, doff + 1, dout_len, 0, 4, 1, nullptr));
+    CZ_CUDA(c, cz_launch_lz4_encode(d, doff, dlen, 1, dout, doff + 1, dout_len, 0, 4, 1, nullptr, nullptr,
+                                    c->lz_effort));
     int n = 0;
     CZ_CUDA(c, cudaMemcpy(&n, dout_len, 4, cudaMemcpyDeviceToHost));
     if (n < 0) return fail(c, CZ_E_CUDA, "LZ4 encoder output exceeded its bound");
@@ -977,7 +988,7 @@ int cz_zlib_compress(cz_ctx *c, const uint8_t *src, int isize, uint8_t *dst, int
     CZ_CUDA(c, cudaMemcpy(meta, h, 32, cudaMemcpyHostToDevice));
     long long *doff = reinterpret_cast<long long *>(meta);
     int *dlen = reinterpret_cast<int *>(meta + 24);
-    CZ_CUDA(c, cz_launch_lz77_parse(d, doff, dlen, 1, dseq, doff + 1, dlen + 1, 0, 1, nullptr));
+    CZ_CUDA(c, cz_launch_lz77_parse(d, doff, dlen, 1, dseq, doff + 1, dlen + 1, 0, 1, nullptr, c->lz_effort));
     CZ_CUDA(c, cz_launch_deflate(d, doff, dlen, dseq, doff + 1, dlen + 1, 1, 0, dz, (long long)zbytes, doff + 2,
                                  dlen + 2, 1, nullptr));
     int n = 0;
@@ -1220,7 +1231,7 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
             const int lzgrid = std::max(1, std::min((n + 31) / 32, c->sms));
             CZ_CUDA(c, cz_launch_lz4_encode(stage, src_off, len, n, lzo, P<long long>(c->lz_off) + f0,
                                             P<int>(c->lz_len) + f0, p->shuffle ? 1 : 0, 32, lzgrid, ls,
-                                            P<int4>(c->lz_hole) + f0));
+                                            P<int4>(c->lz_hole) + f0, c->lz_effort));
             CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len) + f0, n, P<int>(c->flag), ls));
             CZ_CUDA(c, cudaEventRecord(c->ev_lz[i], ls));
             src = lzo;

@@ -56,15 +56,19 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 // length, 0} of one literal-only span (byte planes 1 and 2 of a record
 // chunk) that the encoder leaves unwritten in its output for the gather to
 // copy from the input; length 0 when there is none.
+// effort: 0 the lane-parallel parse alone; 1 (default) also extends matches
+// backwards over equal bytes and keeps the tail of a match that a lower
+// lane's match overlaps; 2 also takes repeats at distance 1-3 that the hash
+// table misses and starts each lane's walk 8 positions early.
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
-                                 int grid, cudaStream_t st, int4 *hole = nullptr);
+                                 int grid, cudaStream_t st, int4 *hole = nullptr, int effort = 1);
 // The LZ77 parse of the LZ4 encoder for DEFLATE: distances up to 32 KiB,
 // 8-byte sequence records (zl::seq_pack) per chunk at seq + seq_off[c]
 // (capacity 8 * (in_len/4 + 2) bytes); seq_bytes[c] = record bytes.
 cudaError_t cz_launch_lz77_parse(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *seq, const long long *seq_off, int *seq_bytes, int records, int grid,
-                                 cudaStream_t st);
+                                 cudaStream_t st, int effort = 1);
 // zlib streams (RFC 1950/1951) from the parse: chunk c at out + c * out_slot
 // (out_slot >= cz_zlib_bound of the chunk), out_off[c] = c * out_slot,
 // out_len[c] = stream bytes, -1 for a bad parse, -2..-4 for an internal

@@ -166,7 +166,7 @@ __device__ __forceinline__ void next_skip(Skip &k, const uint8_t *src, int L)
 //   emit   -- every lane sizes its kept sequences, a warp scan places them,
 //             every lane writes its own; literal runs longer than 32 bytes
 //             are queued and copied by the whole warp.
-constexpr int kSW = 512, kSub = kSW / 32, kMaxSeqLane = kSub / 4;
+constexpr int kSW = 512, kSub = kSW / 32, kMaxSeqLane = kSub / 4, kOvl = 8;
 constexpr int kMinHole = 256;  // smallest literal-only span left to the gather
 // Hash table entry: position modulo 2^18 in the high bits, a 14-bit tag of
 // the 4-byte sequence in the low bits. A tag hit is only a candidate: the
@@ -217,6 +217,29 @@ __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, in
     return len < matchlimit - p ? len : matchlimit - p;
 }
 
+// match_len from byte 0, and how many of the (at most 4) bytes before p
+// equal the bytes before cand (0 when cand < 4): the words before both
+// positions are loaded with the first 8 bytes, so the count costs no
+// extra round trip to memory.
+__device__ __forceinline__ int match_len_back(const uint8_t *src, int p, int cand, int matchlimit, int &back)
+{
+    const uintptr_t pa = reinterpret_cast<uintptr_t>(src + p), ca = reinterpret_cast<uintptr_t>(src + cand);
+    const uint32_t *pw = reinterpret_cast<const uint32_t *>(pa & ~(uintptr_t)3);
+    const uint32_t *cw = reinterpret_cast<const uint32_t *>(ca & ~(uintptr_t)3);
+    const uint32_t ps = (uint32_t)(pa & 3) * 8, cs = (uint32_t)(ca & 3) * 8;
+    const bool before = cand >= 4;  // then p > cand >= 4 too: both words lie inside the chunk
+    const uint32_t p0 = pw[0], p1 = pw[1], p2 = pw[2], pm = before ? pw[-1] : 0u;
+    const uint32_t c0 = cw[0], c1 = cw[1], c2 = cw[2], cm = before ? cw[-1] : 0u;
+    const uint32_t a0 = ps ? __funnelshift_r(p0, p1, ps) : p0, a1 = ps ? __funnelshift_r(p1, p2, ps) : p1;
+    const uint32_t b0 = cs ? __funnelshift_r(c0, c1, cs) : c0, b1 = cs ? __funnelshift_r(c1, c2, cs) : c1;
+    const uint32_t ab = ps ? __funnelshift_r(pm, p0, ps) : pm, bb = cs ? __funnelshift_r(cm, c0, cs) : cm;
+    back = before ? __clz(ab ^ bb) >> 3 : 0;
+    const uint32_t x0 = a0 ^ b0, x1 = a1 ^ b1;
+    const int k = x0 ? (__ffs(x0) - 1) >> 3 : x1 ? 4 + ((__ffs(x1) - 1) >> 3) : 8;
+    if (k < 8) return k < matchlimit - p ? k : matchlimit - p;
+    return match_len(src, p, cand, 8, matchlimit);
+}
+
 // SEQ: the parse for the DEFLATE encoder instead of LZ4 bytes -- distances up
 // to 32 KiB, and per kept sequence one 8-byte record (literal run, match
 // length, distance; zl::seq_pack) at out + out_off[c]; the last record holds
@@ -225,17 +248,18 @@ __device__ __forceinline__ int match_len(const uint8_t *src, int p, int cand, in
 struct LzEncWarp {
     uint32_t table[1 << kHashLog];
     int4 longq[32];                   // (dst offset, src offset, n, -)
-    uint32_t seq[32][kMaxSeqLane];    // start - base | offset << 16
+    uint32_t seq[32][kMaxSeqLane];    // start - base | back extension << 12 | offset << 16
     int lens[32][kMaxSeqLane];
     uint16_t info[kSW];               // candidate offset per position, 0: none
     int nlong;
 };
 
-template <int kLzWarps, bool SEQ>
+template <int kLzWarps, bool SEQ, int kEffort>
 __global__ void __launch_bounds__(kLzWarps * 32)
 lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
                   uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records, int4 *hole)
 {
+    constexpr bool kThorough = kEffort >= 2;
     constexpr int kMaxOff = SEQ ? zl::kMaxDist : 65535;
     // up to 8 warps in static shared memory; 32 (a whole SM) in dynamic
     extern __shared__ __align__(16) unsigned char lz_enc_smem[];
@@ -288,6 +312,11 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             bool any_match = false;
             constexpr int kSteps = (kSW + 4 + 127) / 128;
             uint32_t wv[kSteps], wx[kSteps];
+            // effort 2: the word before the window (for the distance 1-3
+            // candidates of its first positions)
+            uint32_t wprev = kThorough && (base & ~3) >= 4
+                                 ? __ldg(reinterpret_cast<const uint32_t *>(src + (base & ~3) - 4))
+                                 : 0u;
 #pragma unroll
             for (int k = 0; k < kSteps; ++k) {
                 const int wpos = (base & ~3) + 128 * k + 4 * lane;
@@ -304,15 +333,25 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 const uint32_t w0 = wv[k];
                 uint32_t w1 = __shfl_down_sync(0xffffffffu, w0, 1);
                 if (lane == 31) w1 = wx[k];
-                uint32_t seq[4], h[4];
+                // sx[3 + i]: the 4-byte sequence at wpos + i, i = -3..3
+                // (i < 0 only with effort 2)
+                uint32_t sx[7], h[4];
                 bool valid[4];
+                if (kThorough) {
+                    uint32_t wp = __shfl_up_sync(0xffffffffu, w0, 1);
+                    if (lane == 0) wp = wprev;
+                    wprev = __shfl_sync(0xffffffffu, w0, 31);
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) sx[i] = __funnelshift_r(wp, w0, 8 + 8 * i);
+                }
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int p = wpos + j;
                     valid[j] = p >= base && p < end;
-                    seq[j] = j ? __funnelshift_r(w0, w1, 8 * j) : w0;
-                    h[j] = lz_hash(seq[j]);
+                    sx[3 + j] = j ? __funnelshift_r(w0, w1, 8 * j) : w0;
+                    h[j] = lz_hash(sx[3 + j]);
                 }
+                const uint32_t *seq = sx + 3;
                 uint32_t e[4], tag[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -331,6 +370,13 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     int v = 0;
                     if (valid[j] && e[j] != kEmpty && (e[j] & 0x3fff) == tag[j] && off >= 1 && off <= kMaxOff && off <= p)
                         v = off;  // the walk verifies and measures chosen candidates
+                    if (kThorough) {
+                        // the table is read before this step's positions
+                        // enter it, so a repeat at distance 1-3 (runs, short
+                        // periods) is taken from the sequences directly
+                        const int near = seq[j] == sx[2 + j] ? 1 : seq[j] == sx[1 + j] ? 2 : seq[j] == sx[j] ? 3 : 0;
+                        if (near && p >= near) v = near;
+                    }
                     if (valid[j]) info[p - base] = (uint16_t)v;
                     any_match |= v != 0;
                 }
@@ -343,28 +389,44 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             }
             miss = 0;
             // ---- walk: lane-local greedy parse of [base + kSub*lane, +kSub)
-            int ns = 0, first_start = 0x7fffffff, last_start = -1, last_end = -1;
+            // (effort 2: entered kOvl positions early, at the end of the
+            // lower lane's segment, so that it mostly lands on the serial
+            // parse's path); a kept match also records how many bytes before
+            // it equal the bytes before its source (at most 4), taken into
+            // the match in the emission as far as the literal run allows
+            // (effort >= 1: lz4.c's backward "catch up", lz4.c:586-587)
+            int ns = 0, last_start = -1, last_end = -1;
             {
                 const int w0p = base + kSub * lane;
-                int q = w0p;
+                int q = kThorough && lane ? w0p - kOvl : w0p;
                 const int qe = min(w0p + kSub, end);
                 while (q < qe) {
                     const int off = info[q - base];
-                    const int len = off ? match_len(src, q, q - off, 0, matchlimit) : 0;
+                    int ext = 0;
+                    const int len = !off ? 0
+                                    : kEffort >= 1 ? match_len_back(src, q, q - off, matchlimit, ext)
+                                                   : match_len(src, q, q - off, 0, matchlimit);
                     if (len >= kMinMatch) {
-                        myseq[ns] = (uint32_t)(q - base) | (uint32_t)off << 16;
-                        mylen[ns] = len;
-                        ++ns;
-                        if (first_start > q) first_start = q;
-                        last_start = q;
-                        last_end = q + len;
+                        if (q >= w0p) {
+                            myseq[ns] = (uint32_t)(q - base) | (uint32_t)ext << 12 | (uint32_t)off << 16;
+                            mylen[ns] = len;
+                            ++ns;
+                            last_start = q;
+                            last_end = q + len;
+                        }
                         q += len;
                     } else {
                         ++q;
                     }
                 }
             }
-            // ---- merge: P_k = end of the last kept match of lanes < k.
+            // ---- merge: P_k = end of the last kept match of lanes < k. With
+            // effort >= 1 a match [s, e) that starts before the literal
+            // position P is kept from P on when that part is still a match
+            // (>= 4 bytes) that may follow a literal run (P <= mflimit).
+            auto survives = [&](int s, int e, int P) {
+                return s >= P || (kEffort >= 1 && e - P >= kMinMatch && P <= mflimit);
+            };
             // Usually every lane keeps its last sequence, so P_k is the end
             // of the nearest lower lane's last match; where a match reaches
             // past a later lane's last start, the exact serial rule runs.
@@ -373,7 +435,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             int myP = __shfl_sync(0xffffffffu, last_end, lower ? 31 - __clz(lower) : 0);
             if (!lower) myP = anchor;
             int P = has ? __shfl_sync(0xffffffffu, last_end, 31 - __clz(has)) : anchor;
-            const unsigned bad = __ballot_sync(0xffffffffu, ns > 0 && last_start < myP);
+            const unsigned bad = __ballot_sync(0xffffffffu, ns > 0 && !survives(last_start, last_end, myP));
             if (bad) {
                 // lanes below the first failing one are exact; from there the
                 // serial rule over the lanes that have sequences
@@ -384,17 +446,18 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     const int ls = __shfl_sync(0xffffffffu, last_start, k);
                     const int le = __shfl_sync(0xffffffffu, last_end, k);
                     if (lane == k) myP = P;
-                    if (ls >= P) P = le;
+                    if (survives(ls, le, P)) P = le;
                 }
             }
             // ---- emit: kept sequences are those starting at or after myP
             int lit_from = myP, bytes = 0, nkeep = 0;
             for (int i = 0; i < ns; ++i) {
-                const int st = base + (int)(myseq[i] & 0xffff);
-                if (st < lit_from) continue;
-                const int l = st - lit_from, ml = mylen[i] - kMinMatch;
+                const int s0 = base + (int)(myseq[i] & 0xfff);
+                if (!survives(s0, s0 + mylen[i], lit_from)) continue;
+                const int st = max(s0 - (int)((myseq[i] >> 12) & 7), lit_from);
+                const int l = st - lit_from, ml = s0 + mylen[i] - st - kMinMatch;
                 bytes += SEQ ? 8 : 1 + (l >= 15 ? len_bytes(l - 15) : 0) + l + 2 + (ml >= 15 ? len_bytes(ml - 15) : 0);
-                lit_from = st + mylen[i];
+                lit_from = s0 + mylen[i];
                 ++nkeep;
             }
             int incl = bytes;
@@ -414,20 +477,22 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 int at = op + incl - bytes;
                 lit_from = myP;
                 for (int i = 0; i < ns; ++i) {
-                    const int st = base + (int)(myseq[i] & 0xffff);
-                    if (st < lit_from) continue;
+                    const int s0 = base + (int)(myseq[i] & 0xfff);
+                    if (!survives(s0, s0 + mylen[i], lit_from)) continue;
+                    const int st = max(s0 - (int)((myseq[i] >> 12) & 7), lit_from);
                     *reinterpret_cast<unsigned long long *>(dst + at) =
-                        zl::seq_pack(st - lit_from, mylen[i], (int)(myseq[i] >> 16));
+                        zl::seq_pack(st - lit_from, s0 + mylen[i] - st, (int)(myseq[i] >> 16));
                     at += 8;
-                    lit_from = st + mylen[i];
+                    lit_from = s0 + mylen[i];
                 }
             } else {
                 int at = op + incl - bytes;
                 lit_from = myP;
                 for (int i = 0; i < ns; ++i) {
-                    const int st = base + (int)(myseq[i] & 0xffff);
-                    if (st < lit_from) continue;
-                    const int l = st - lit_from, ml = mylen[i] - kMinMatch, off = (int)(myseq[i] >> 16);
+                    const int s0 = base + (int)(myseq[i] & 0xfff);
+                    if (!survives(s0, s0 + mylen[i], lit_from)) continue;
+                    const int st = max(s0 - (int)((myseq[i] >> 12) & 7), lit_from);
+                    const int l = st - lit_from, ml = s0 + mylen[i] - st - kMinMatch, off = (int)(myseq[i] >> 16);
                     uint8_t *d = dst + at;
                     *d++ = (uint8_t)(((l >= 15 ? 15 : l) << 4) | (ml >= 15 ? 15 : ml));
                     if (l >= 15) {
@@ -445,7 +510,7 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     d[1] = (uint8_t)(off >> 8);
                     if (ml >= 15) put_len_serial(d + 2, ml - 15);
                     at += 1 + (l >= 15 ? len_bytes(l - 15) : 0) + l + 2 + (ml >= 15 ? len_bytes(ml - 15) : 0);
-                    lit_from = st + mylen[i];
+                    lit_from = s0 + mylen[i];
                 }
             }
             __syncwarp();
@@ -934,13 +999,13 @@ using namespace cz;
 // kLzWarps chunks per CTA; 32 fills an SM (1024 threads, ~210 KB of shared
 // memory), so that CTAs of this kernel and the wavelet kernel, which also
 // takes a whole SM, share the machine SM by SM.
-template <int W, bool SEQ>
-static cudaError_t launch_enc(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
-                              uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
-                              cudaStream_t st, int4 *hole = nullptr)
+template <int W, bool SEQ, int E>
+static cudaError_t launch_enc_t(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
+                                uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
+                                cudaStream_t st, int4 *hole)
 {
     const int sm = W <= 8 ? 0 : (int)sizeof(LzEncWarp) * W;
-    auto k = lz4_encode_kernel<W, SEQ>;
+    auto k = lz4_encode_kernel<W, SEQ, E>;
     if (sm > 48 * 1024) {
         const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         if (e != cudaSuccess) return e;
@@ -949,28 +1014,47 @@ static cudaError_t launch_enc(const uint8_t *in, const long long *in_off, const 
     return cudaGetLastError();
 }
 
+// one kernel per effort level, so that a level pays only for its own work
+template <int W, bool SEQ>
+static cudaError_t launch_enc(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
+                              uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
+                              cudaStream_t st, int4 *hole, int effort)
+{
+    switch (effort) {
+    case 0:
+        return launch_enc_t<W, SEQ, 0>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+    case 2:
+        return launch_enc_t<W, SEQ, 2>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+    default:
+        return launch_enc_t<W, SEQ, 1>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+    }
+}
+
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, int *out_len, int records, int warps,
-                                 int grid, cudaStream_t st, int4 *hole)
+                                 int grid, cudaStream_t st, int4 *hole, int effort)
 {
     if (nchunks <= 0) return cudaSuccess;
     switch (warps) {
-    case 2: return launch_enc<2, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
-    case 8: return launch_enc<8, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+    case 2:
+        return launch_enc<2, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
+    case 8:
+        return launch_enc<8, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
     case 16:
-        return launch_enc<16, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+        return launch_enc<16, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
     case 32:
-        return launch_enc<32, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
-    default: return launch_enc<4, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
+        return launch_enc<32, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
+    default:
+        return launch_enc<4, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
     }
 }
 
 cudaError_t cz_launch_lz77_parse(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *seq, const long long *seq_off, int *seq_bytes, int records, int grid,
-                                 cudaStream_t st)
+                                 cudaStream_t st, int effort)
 {
     if (nchunks <= 0) return cudaSuccess;
-    return launch_enc<4, true>(in, in_off, in_len, nchunks, seq, seq_off, seq_bytes, records, grid, st);
+    return launch_enc<4, true>(in, in_off, in_len, nchunks, seq, seq_off, seq_bytes, records, grid, st, nullptr, effort);
 }
 
 cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,

@@ -100,6 +100,20 @@ const char *cz_last_error(cz_ctx *ctx);
 int cz_set_timing(cz_ctx *ctx, int on);
 int cz_stage_times(cz_ctx *ctx, float *ms, int n);
 
+/* Parse effort of the GPU LZ4 encoder (and of the LZ77 parse under the zlib
+ * stage) for the context's later calls; plans keep the effort they were
+ * created with. Any level yields streams that the reference decoder reads
+ * (lz4.c:802-905); higher levels find more matches and take longer:
+ *   0  the lane-parallel greedy parse alone (fastest)
+ *   1  (default) also extends matches backwards over equal bytes, as
+ *      lz4.c's "catch up" does (lz4.c:586-587), and keeps the part of a
+ *      match that the match of a lower lane overlaps
+ *   2  also takes repeats at distance 1-3 that the hash table misses, and
+ *      starts each lane's walk 8 positions early
+ * CZ_E_ARG for other values. No counterpart in the reference, whose LZ4 has
+ * one level. */
+int cz_set_lz4_effort(cz_ctx *ctx, int effort);
+
 /* ---- per-block drop-in (host buffers) --------------------------------- */
 /* WaveletCompressor::compress of one 32^3 block in[z][y][x]: writes the
  * record [4096-byte mask][survivors] to out (capacity CZ_MAX_RECORD) and its

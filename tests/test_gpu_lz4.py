@@ -116,3 +116,49 @@ def test_gpu_lz4_returns_the_reference_decoder_results(cz):
         if ref > 0:
             assert hashlib.sha256(dst[:ref].tobytes()).hexdigest() == ref_sha
 
+
+
+def test_gpu_lz4_effort_levels(cz, small_field):
+    """Every parse effort writes streams that the restated reference decoder
+    and the GPU decoder read back exactly, on the round-trip samples and on
+    a field's record chunks (also through the image writer's pipelined path
+    and the zlib stage's LZ77 parse); on the record chunks a higher effort
+    never writes more bytes."""
+    import torch
+    rng = np.random.default_rng(5)
+    raw, roff = O.field_compress(small_field, 1e-3, 1, 4, 1, 0, 1)
+    toks = [rng.integers(0, 8, 7, np.uint8).tobytes() for _ in range(40)]
+    samples = [b"", bytes(13), rng.integers(0, 256, 5000, np.uint8).tobytes(), b"ab" * 3000 + b"abc" * 2000,
+               b"".join(toks[i] for i in rng.integers(0, 40, 20000)), bytes(raw[roff[3]:roff[4]])]
+    ref_field = O.field_decompress(raw, roff, small_field.shape, 1, 1)
+    f = torch.from_numpy(small_field).cuda()
+    ctx = cz.context(0)
+    sizes = []
+    try:
+        for effort in (0, 1, 2):
+            ctx.set_lz4_effort(effort)
+            for d in samples:
+                z = cz.lz4_compress(d)
+                n, out = O.lz4_decompress(z, len(d))
+                assert n == len(d) and out.tobytes() == d
+                assert cz.lz4_decompress(z, len(d)) == d
+            cf = cz.compress_field(f, 1e-3, 1, 4, True, encoder="lz4")
+            data, off = cf.to_device()
+            o, dd = off.cpu().numpy(), data.cpu().numpy()
+            for c in range(len(o) - 1):
+                n, out = O.lz4_decompress(dd[o[c]:o[c + 1]], int(roff[c + 1] - roff[c]))
+                assert n == roff[c + 1] - roff[c] and np.array_equal(out, raw[roff[c]:roff[c + 1]])
+            sizes.append(int(o[-1]))
+            dec = cz.decompress_field(data, off, small_field.shape, 1, True, encoder="lz4").cpu().numpy()
+            assert np.array_equal(dec, ref_field)
+            img = cz.compress_to_image(small_field, 1e-3, 1, 4, True, encoder="lz4")
+            assert np.array_equal(cz.decompress_image(img, 1, True), ref_field)
+            cz_ = cz.compress_field(f, 1e-3, 1, 4, True, encoder="zlib")
+            zd, zo = cz_.to_device()
+            dec = cz.decompress_field(zd, zo, small_field.shape, 1, True, encoder="zlib").cpu().numpy()
+            assert np.array_equal(dec, ref_field)
+        with pytest.raises(cz.CzError):
+            ctx.set_lz4_effort(3)
+    finally:
+        ctx.set_lz4_effort(1)
+    assert sizes[1] <= sizes[0] and sizes[2] <= sizes[1], sizes
