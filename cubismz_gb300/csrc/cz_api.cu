@@ -383,6 +383,11 @@ int decompress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long n
                                       dcap, raw, st));
     const uint8_t *base = d_data;
     const int *dlen = P<int>(c->in_len);
+    // one shuffled record per chunk, blocks in chunk order: the LZ4 decoder
+    // may leave the records' byte planes 1 and 2 in its input, where the
+    // decode kernel reads them
+    const bool planes_in_input = bpc == 1 && shuffle && !h_block_chunk && (long long)nchunks == nblocks;
+    CzPlanes planes;
     if (encoder == CZ_ENCODER_ZLIB) {
         CZ_CUDA(c, cz_launch_inflate(d_data, d_off, P<int>(c->in_len), nchunks, P<uint8_t>(c->dec),
                                      P<long long>(c->dec_off), P<int>(c->dec_cap), P<int>(c->dec_len),
@@ -391,8 +396,13 @@ int decompress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long n
         dlen = P<int>(c->dec_len);
     } else if (!raw) {
         const int lzgrid = std::max(1, std::min((nchunks + 3) / 4, c->sms * 8));
+        if (planes_in_input) {
+            CZ_TRY(grow(c, c->lz_hole, sizeof(int4) * (size_t)nchunks));
+            planes = CzPlanes{P<int4>(c->lz_hole), d_data, d_off};
+        }
         CZ_CUDA(c, cz_launch_lz4_decode(d_data, d_off, P<int>(c->in_len), nchunks, P<uint8_t>(c->dec),
-                                        P<long long>(c->dec_off), P<int>(c->dec_cap), P<int>(c->dec_len), lzgrid, st));
+                                        P<long long>(c->dec_off), P<int>(c->dec_cap), P<int>(c->dec_len), lzgrid, st,
+                                        planes_in_input ? P<int4>(c->lz_hole) : nullptr));
         base = P<uint8_t>(c->dec);
         dlen = P<int>(c->dec_len);
     }
@@ -420,7 +430,7 @@ int decompress_fields(cz_ctx *c, const std::vector<CzField> &fields, long long n
     double *per_block = diff_ref ? P<double>(c->diff) : nullptr;
     CZ_CUDA(c, cz_launch_decode(wtype, P<CzField>(c->fields), (int)fields.size(), nblocks, shuffle ? 1 : 0, base,
                                 P<long long>(c->rec_off), P<int>(c->status), P<unsigned long long>(c->queue), grid,
-                                st, diff_ref, per_block));
+                                st, diff_ref, per_block, planes));
     if (diff_ref) CZ_CUDA(c, cz_launch_diff_total(per_block, nblocks, per_block + 8 * nblocks, st));
     CZ_TRY(mark(c, 3, st));
     CZ_CUDA(c, cz_launch_status_reduce(P<int>(c->status), nblocks, P<int>(c->flag), st));

@@ -356,14 +356,25 @@ __device__ __forceinline__ void runs_from_mask(const Shared &s)
     }
 }
 
+// n bytes from p into L2, one 128-byte line per thread and step (a hint:
+// nothing is read into registers)
+__device__ __forceinline__ void prefetch_l2_span(const uint8_t *p, int n)
+{
+    const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)127;
+    const uintptr_t a1 = reinterpret_cast<uintptr_t>(p) + (uintptr_t)(n > 0 ? n : 0);
+    for (uintptr_t a = a0 + 128 * (uintptr_t)threadIdx.x; a < a1; a += 128 * (uintptr_t)blockDim.x)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+}
+
 struct Payload {
     const uint8_t *p;
-    int c;  // byte-plane stride (reshuffle3's n/4, WaveletCompressor.cpp:80)
+    const uint8_t *q;  // byte planes 1 and 2 (p + c, or where the LZ4 stage left them)
+    int c;             // byte-plane stride (reshuffle3's n/4, WaveletCompressor.cpp:80)
     bool shuffle;
     __device__ __forceinline__ float get(int k) const
     {
         if (shuffle)
-            return __uint_as_float((uint32_t)p[k] | ((uint32_t)p[c + k] << 8) | ((uint32_t)p[2 * c + k] << 16) |
+            return __uint_as_float((uint32_t)p[k] | ((uint32_t)q[k] << 8) | ((uint32_t)q[c + k] << 16) |
                                    ((uint32_t)p[3 * c + k] << 24));
         return __uint_as_float(reinterpret_cast<const uint32_t *>(p)[k]);
     }

@@ -202,7 +202,7 @@ template <int KIND, bool DIFF>
 __global__ void __launch_bounds__(kNT, 1)
 decode_kernel(const CzField *fields, int nfields, long long total_blocks, int shuffle, const uint8_t *base,
               const long long *rec_off, int *status, unsigned long long *queue, const float *diff_ref,
-              double *diff_out)
+              double *diff_out, CzPlanes planes)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const Shared s = carve(smem);
@@ -223,6 +223,24 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
         const uint8_t *slot = base + (ro < 0 ? 0 : ro);
         const int nb = ro < 0 ? -1 : *reinterpret_cast<const int *>(slot);
         const bool size_ok = nb >= kMaskBytes && nb <= kMaxRecord + 4;
+        // the payload into L2 while the mask is read and scanned (byte
+        // planes 1 and 2 from the LZ4 input where the LZ4 stage left them)
+        const uint8_t *q12 = nullptr;
+        if (size_ok) {
+            const uint8_t *pay = slot + 4 + kMaskBytes;
+            const int np = nb - kMaskBytes, c4 = np / 4;
+            if (planes.hole && shuffle) {
+                const int4 h = planes.hole[g];
+                if (h.z > 0 && h.z == 2 * c4 && h.x == 4 + kMaskBytes + c4) q12 = planes.src + planes.src_off[g] + h.y;
+            }
+            if (q12) {
+                prefetch_l2_span(pay, c4);
+                prefetch_l2_span(q12, 2 * c4);
+                prefetch_l2_span(pay + 3 * c4, np - 3 * c4);
+            } else {
+                prefetch_l2_span(pay, np);
+            }
+        }
         // deserialize_bitset (WaveletCompressor.cpp:124-150)
         for (int i = threadIdx.x; i < kMaskBytes / 4; i += kNT)
             s.mask32[i] = size_ok ? reinterpret_cast<const uint32_t *>(slot + 4)[i] : 0u;
@@ -248,6 +266,7 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
             Payload pl;
             pl.p = slot + 4 + kMaskBytes;
             pl.c = payload / 4;
+            pl.q = q12 ? q12 : pl.p + pl.c;  // planes 1 and 2
             pl.shuffle = shuffle != 0;
             load_survivors(s, expected, [&](int k) { return pl.get(k); });
         } else {
@@ -385,13 +404,13 @@ template <int KIND>
 static cudaError_t launch_decode(const CzField *fields, int nfields, long long total_blocks, int shuffle,
                                  const uint8_t *base, const long long *rec_off, int *status,
                                  unsigned long long *queue, int grid, cudaStream_t st, const float *diff_ref,
-                                 double *diff_out)
+                                 double *diff_out, CzPlanes planes)
 {
     auto k = diff_ref ? decode_kernel<KIND, true> : decode_kernel<KIND, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes);
     if (e != cudaSuccess) return e;
     k<<<grid, kNT, kSmBytes, st>>>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, diff_ref,
-                                   diff_out);
+                                   diff_out, planes);
     return cudaGetLastError();
 }
 
@@ -414,18 +433,18 @@ cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long
 
 cudaError_t cz_launch_decode(int wtype, const CzField *fields, int nfields, long long total_blocks, int shuffle,
                              const uint8_t *base, const long long *rec_off, int *status, unsigned long long *queue,
-                             int grid, cudaStream_t st, const float *diff_ref, double *diff_out)
+                             int grid, cudaStream_t st, const float *diff_ref, double *diff_out, CzPlanes planes)
 {
     switch (wkind(wtype)) {
     case 1:
         return launch_decode<1>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st,
-                                diff_ref, diff_out);
+                                diff_ref, diff_out, planes);
     case 2:
         return launch_decode<2>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st,
-                                diff_ref, diff_out);
+                                diff_ref, diff_out, planes);
     default:
         return launch_decode<3>(fields, nfields, total_blocks, shuffle, base, rec_off, status, queue, grid, st,
-                                diff_ref, diff_out);
+                                diff_ref, diff_out, planes);
     }
 }
 

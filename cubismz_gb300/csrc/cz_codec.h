@@ -25,9 +25,18 @@ cudaError_t cz_launch_encode(int wtype, const CzField *fields, int nfields, long
 // negative rec_off marks a block whose record is missing (status -1).
 // diff_ref (optional, a field of the same geometry as fields[0]): per-block
 // error statistics into diff_out[8*g] (cz2diff's quantities).
+// Byte planes 1 and 2 of one-record chunks left in the LZ4 input by
+// cz_launch_lz4_decode (hole per chunk = per block, chunk c at src +
+// src_off[c]); hole == nullptr: every record is whole.
+struct CzPlanes {
+    const int4 *hole = nullptr;
+    const uint8_t *src = nullptr;
+    const long long *src_off = nullptr;
+};
 cudaError_t cz_launch_decode(int wtype, const CzField *fields, int nfields, long long total_blocks, int shuffle,
                              const uint8_t *base, const long long *rec_off, int *status, unsigned long long *queue,
-                             int grid, cudaStream_t st, const float *diff_ref = nullptr, double *diff_out = nullptr);
+                             int grid, cudaStream_t st, const float *diff_ref = nullptr, double *diff_out = nullptr,
+                             CzPlanes planes = CzPlanes());
 cudaError_t cz_launch_diff_total(const double *per_block, long long nblocks, double *total, cudaStream_t st);
 
 // Linear inverse transform and its adjoint on stacked 32^3 blocks; block
@@ -78,9 +87,14 @@ cudaError_t cz_launch_deflate(const uint8_t *in, const long long *in_off, const 
                               const long long *seq_off, const int *seq_bytes, int nchunks, int records,
                               uint8_t *out, long long out_slot, long long *out_off, int *out_len, int grid,
                               cudaStream_t st);
+// hole (optional; one-record chunks of shuffled records only): written for
+// every chunk; {out position, input position, length, 0} of the record's
+// byte planes 1 and 2 when one literal run covers them whole -- the decoder
+// then leaves that span of its output unwritten and the record's reader
+// takes it from the input (CzPlanes); length 0 otherwise.
 cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, const int *out_cap, int *out_len, int grid,
-                                 cudaStream_t st);
+                                 cudaStream_t st, int4 *hole = nullptr);
 
 // Stream assembly helpers (cz_lz4.cu, cz_stream.cu)
 // With hole (from cz_launch_lz4_encode): the span of each chunk that the

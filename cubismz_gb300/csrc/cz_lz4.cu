@@ -634,11 +634,26 @@ __device__ __forceinline__ void copy_lit(uint8_t *ring, int o, const uint8_t *s,
 // byte-serial copy repeats the first `off` bytes when off < length.
 __device__ __forceinline__ int msrc(int k, int off, int ml) { return off >= ml ? k : k % off; }
 
-// Output byte x, x < the window's start: from the ring when it is still
-// held there (x >= lo), else from the output in global memory (via L2).
-__device__ __forceinline__ uint8_t out_byte(const uint8_t *ring, const uint8_t *dst, int x, int lo)
+// Byte planes 1 and 2 of a record chunk that the decoder left in its input
+// (a literal run it did not copy): output [out, out + len) is input
+// [in, in + len); len 0: none.
+struct LzHole {
+    int out = 0, len = 0, in = 0;
+};
+
+// Output byte x from global memory: from the input inside the hole, else
+// from the output (via L2).
+__device__ __forceinline__ uint8_t old_byte(const uint8_t *src, const uint8_t *dst, const LzHole &h, int x)
 {
-    return x >= lo ? ring[x & kMask] : __ldcg(dst + x);
+    return (unsigned)(x - h.out) < (unsigned)h.len ? __ldg(src + h.in + (x - h.out)) : __ldcg(dst + x);
+}
+
+// Output byte x, x < the window's start: from the ring when it is still
+// held there (x >= lo), else from global memory.
+__device__ __forceinline__ uint8_t out_byte(const uint8_t *ring, const uint8_t *src, const uint8_t *dst,
+                                            const LzHole &h, int x, int lo)
+{
+    return x >= lo ? ring[x & kMask] : old_byte(src, dst, h, x);
 }
 
 // ml <= 8 bytes of a match at ms whose sources lie before the window and
@@ -674,7 +689,8 @@ __device__ __forceinline__ void flush(uint8_t *d, const uint8_t *ring, int r, in
 
 __global__ void __launch_bounds__(128)
 lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
-                  uint8_t *__restrict__ out, const long long *out_off, const int *out_cap, int *out_len)
+                  uint8_t *__restrict__ out, const long long *out_off, const int *out_cap, int *out_len,
+                  int4 *hole)
 {
     __shared__ int4 cand_all[4][kWin];           // (literal start, literal length, match length, offset | flags)
     __shared__ int next_all[4][kWin];            // input position after the candidate's sequence
@@ -697,6 +713,34 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
         const int oend = out_cap[c];
         int s0 = 0, op = 0, err = 0, ring_lo = 0;  // output before ring_lo is not in the ring
         bool done = false;
+        LzHole hl;
+        if (hole && lane == 0) hole[c] = make_int4(0, 0, 0, 0);  // written for every chunk
+        // a literal run of n bytes from input i to output o, except the
+        // record's byte planes 1 and 2 when it covers them whole (hole
+        // given, record chunks: the record's byte count is output bytes 0-3)
+        auto lit_run = [&](int o, int i, int n) {
+            int a = 0, b = 0;
+            if (hole && hl.len == 0 && o >= 4) {
+                const int nb = (int)__ldcg(dst) | (int)__ldcg(dst + 1) << 8 | (int)__ldcg(dst + 2) << 16 |
+                               (int)__ldcg(dst + 3) << 24;
+                if (nb >= 4096 && nb <= 4096 + 4 * 32768 && ((nb - 4096) & 3) == 0) {
+                    const int S = (nb - 4096) >> 2;
+                    a = 4 + 4096 + S;
+                    b = a + 2 * S;
+                    if (!(o <= a && o + n >= b && b - a >= kMinHole)) a = b = 0;
+                }
+            }
+            if (b > a) {
+                warp_copy(dst + o, src + i, a - o, lane);
+                warp_copy(dst + b, src + i + (b - o), o + n - b, lane);
+                hl.out = a;
+                hl.len = b - a;
+                hl.in = i + (a - o);
+                if (lane == 0) hole[c] = make_int4(hl.out, hl.in, hl.len, 0);
+            } else {
+                warp_copy(dst + o, src + i, n, lane);
+            }
+        };
         if (iend <= 0) {
             if (lane == 0) out_len[c] = 0;  // lz4.c:836: error exit at position 0
             continue;
@@ -855,22 +899,37 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 for (int k = lane; k < n0; k += 32) ring[(o0 + k) & kMask] = __ldg(src + x0 + k);
             }
             // matches whose sources lie before the window and are still in
-            // the ring are copied by their lane; the others replay in order
-            // (in-window sources, sources in global memory, long matches)
+            // the ring are copied by their lane; then, in rounds, every
+            // short match whose source ends before the output of the first
+            // match still to do (so that all of it is written) is copied by
+            // its lane, and when there is none, that first match replays
+            // with the whole warp (long matches, sources in global memory)
             const int lo = max(ring_lo, op + kStage - kRing);  // not overwritten by this window
             const bool fast = mat && q.z <= 8 && ms - off + min(q.z, off) <= op && ms - off >= lo;
             if (fast) copy_match(ring, ms, off, q.z);
             __syncwarp();
-            pend = __ballot_sync(0xffffffffu, mat && !fast);
+            bool todo = mat && !fast;
+            pend = __ballot_sync(0xffffffffu, todo);
             while (pend) {
                 const int who = __ffs(pend) - 1;
-                pend &= pend - 1;
                 const int m0 = __shfl_sync(0xffffffffu, ms, who);
-                const int o0 = __shfl_sync(0xffffffffu, off, who);
-                const int l0 = __shfl_sync(0xffffffffu, q.z, who);
-                for (int k = lane; k < l0; k += 32) {
-                    const int x = m0 - o0 + msrc(k, o0, l0);
-                    ring[(m0 + k) & kMask] = out_byte(ring, dst, x, lo);
+                const bool ready = todo && q.z <= 8 && ms - off + min(q.z, off) <= m0 && ms - off >= lo;
+                const unsigned rb = __ballot_sync(0xffffffffu, ready);
+                if (rb) {  // includes `who` when it is short with its source in the ring
+                    if (ready) {
+                        copy_match(ring, ms, off, q.z);
+                        todo = false;
+                    }
+                    pend &= ~rb;
+                } else {
+                    pend &= pend - 1;
+                    if (lane == who) todo = false;
+                    const int o0 = __shfl_sync(0xffffffffu, off, who);
+                    const int l0 = __shfl_sync(0xffffffffu, q.z, who);
+                    for (int k = lane; k < l0; k += 32) {
+                        const int x = m0 - o0 + msrc(k, o0, l0);
+                        ring[(m0 + k) & kMask] = out_byte(ring, src, dst, hl, x, lo);
+                    }
                 }
                 __syncwarp();
             }
@@ -898,12 +957,12 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     if (ll > (long long)(oend - op) || ll != (long long)(iend - ip)) {
                         err = ip;
                     } else {
-                        warp_copy(dst + op, src + ip, (int)ll, lane);
+                        lit_run(op, ip, (int)ll);
                         op += (int)ll;
                         done = true;
                     }
                 } else {
-                    warp_copy(dst + op, src + ip, (int)ll, lane);
+                    lit_run(op, ip, (int)ll);
                     op += (int)ll;
                     ip += (int)ll;
                     const int o = (int)src[ip] | ((int)src[ip + 1] << 8);
@@ -918,7 +977,8 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                             err = ip;
                         } else {
                             __syncwarp();
-                            for (int k = lane; k < (int)m; k += 32) dst[op + k] = __ldcg(dst + op - o + msrc(k, o, (int)m));
+                            for (int k = lane; k < (int)m; k += 32)
+                                dst[op + k] = old_byte(src, dst, hl, op - o + msrc(k, o, (int)m));
                             __syncwarp();
                             op += (int)m;
                             s0 = ip;
@@ -1059,10 +1119,10 @@ cudaError_t cz_launch_lz77_parse(const uint8_t *in, const long long *in_off, con
 
 cudaError_t cz_launch_lz4_decode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                  uint8_t *out, const long long *out_off, const int *out_cap, int *out_len, int grid,
-                                 cudaStream_t st)
+                                 cudaStream_t st, int4 *hole)
 {
     if (nchunks <= 0) return cudaSuccess;
-    lz4_decode_kernel<<<grid, 128, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_cap, out_len);
+    lz4_decode_kernel<<<grid, 128, 0, st>>>(in, in_off, in_len, nchunks, out, out_off, out_cap, out_len, hole);
     return cudaGetLastError();
 }
 

@@ -124,3 +124,57 @@ def test_all_coefficients_kept(cz, small_field, encoder):
     assert np.array_equal(dec.view(np.uint32), want.view(np.uint32))
     img = cz.compress_to_image(field, -1.0, 1, 0, True, encoder=encoder)
     assert np.array_equal(cz.decompress_image(img, 1, True).view(np.uint32), want.view(np.uint32))
+
+
+def test_lz4_planes_left_in_the_input(cz):
+    """A one-record chunk whose byte planes 1 and 2 sit in one literal run:
+    the LZ4 decoder leaves them in its input and the decode kernel reads
+    them there; the match right after the run and a later one copy from
+    planes 2 and 1, so they read the input too. The decoded block equals
+    the oracle's decode of the record."""
+    import torch
+    from tests.helpers import _lz4_len
+    rng = np.random.default_rng(3)
+    block = rng.standard_normal((32, 32, 32)).astype(np.float32)
+    rec = O.block_compress(block, 0.5, 1, 4, 1)
+    S = (len(rec) - 4096) // 4
+    assert S >= 600
+    chunk = bytearray(np.int32(len(rec)).tobytes()) + bytearray(rec.tobytes())
+    P1, P2, P3 = 4 + 4096 + S, 4 + 4096 + 2 * S, 4 + 4096 + 3 * S
+    for a in (P1, P2, P3, P3 + 12):  # benign bytes: mantissa bits, or an exponent near 1
+        chunk[a:a + 8] = b"\x3f" * 8
+    seen, x, y = {}, None, None
+    for i in range(4, P1 - 8):
+        k = bytes(chunk[i:i + 4])
+        if k in seen:
+            x, y = i, seen[k]
+            break
+        seen.setdefault(k, i)
+    assert x is not None
+    z = bytearray()
+
+    def seq(lits, off, ml):
+        z.append((min(len(lits), 15) << 4) | min(ml - 4, 15))
+        if len(lits) >= 15:
+            _lz4_len(z, len(lits))
+        z.extend(lits)
+        z.extend((off & 255, off >> 8))
+        if ml - 4 >= 15:
+            _lz4_len(z, ml - 4)
+
+    seq(chunk[0:x], x - y, 4)
+    seq(chunk[x + 4:P3], P3 - P2, 8)                # planes 1 and 2 as literals, then a copy of plane 2
+    seq(chunk[P3 + 8:P3 + 12], P3 + 12 - P1, 8)     # a copy of plane 1
+    tail = chunk[P3 + 20:]
+    z.append(min(len(tail), 15) << 4)
+    if len(tail) >= 15:
+        _lz4_len(z, len(tail))
+    z.extend(tail)
+    n, out = O.lz4_decompress(bytes(z), len(chunk))
+    assert n == len(chunk) and out.tobytes() == bytes(chunk)
+    data = torch.from_numpy(np.frombuffer(bytes(z) + bytes(64), np.uint8).copy()).cuda()
+    off = torch.tensor([0, len(z)], dtype=torch.int64, device="cuda")
+    dec = cz.decompress_field(data, off, (32, 32, 32), 1, True, encoder="lz4").cpu().numpy()
+    ref = O.block_decompress(np.frombuffer(bytes(chunk[4:]), np.uint8), 1, 1)
+    assert dec.tobytes() == ref.tobytes()
+    assert cz.lz4_decompress(bytes(z), len(chunk)) == bytes(chunk)
