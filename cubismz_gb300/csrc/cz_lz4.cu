@@ -398,9 +398,30 @@ lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             int ns = 0, last_start = -1, last_end = -1;
             {
                 const int w0p = base + kSub * lane;
-                int q = kThorough && lane ? w0p - kOvl : w0p;
                 const int qe = min(w0p + kSub, end);
+                const int qs = kThorough && lane ? w0p - kOvl : w0p;
+                // the walk's positions that have a candidate (bit i: qs + i),
+                // so that it jumps over literal positions
+                constexpr int kNq = kThorough ? kSub + kOvl : kSub;
+                uint32_t cm = 0;
+                if (qe > qs) {
+                    const uint4 *iv = reinterpret_cast<const uint4 *>(info + (qs - base));  // 16-byte aligned
+#pragma unroll
+                    for (int v = 0; v < kNq / 8; ++v) {
+                        const uint4 a = iv[v];
+                        const uint32_t iw[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            cm |= (uint32_t)((iw[i] & 0xffffu) != 0) << (8 * v + 2 * i) |
+                                  (uint32_t)((iw[i] >> 16) != 0) << (8 * v + 2 * i + 1);
+                    }
+                    if (qe - qs < kNq) cm &= (1u << (qe - qs)) - 1u;
+                }
+                int q = qs;
                 while (q < qe) {
+                    const uint32_t m = cm >> (q - qs);
+                    if (!m) break;
+                    q += __ffs(m) - 1;
                     const int off = info[q - base];
                     int ext = 0;
                     const int len = !off ? 0
