@@ -713,7 +713,7 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                   uint8_t *__restrict__ out, const long long *out_off, const int *out_cap, int *out_len,
                   int4 *hole)
 {
-    __shared__ int4 cand_all[4][kWin];           // (literal start, literal length, match length, offset | flags)
+    __shared__ int4 cand_all[4][kWin];           // (literal start, literal length, match length, flags)
     __shared__ int next_all[4][kWin];            // input position after the candidate's sequence
     __shared__ __align__(16) uint8_t jump_all[4][5][kWin + 4];  // T_b; kExit: leaves the window
     __shared__ __align__(16) uint8_t ring_all[4][kRing + 16];  // recent output (16 bytes of slack)
@@ -771,7 +771,7 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             if (lane < 2 && s0 + kWin + 128 * lane < iend)
                 asm volatile("prefetch.global.L1 [%0];" ::"l"(src + s0 + kWin + 128 * lane));
             {  // phase-major over the 4 candidates, so that their loads overlap
-                int tok[4], ip[4], lit[4], ml[4], off[4], nx[4];
+                int tok[4], ip[4], lit[4], ml[4], nx[4];
                 bool more[4], stat[4];  // stat: a plain sequence so far
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -780,7 +780,6 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     ip[j] = p + 1;
                     lit[j] = (tok[j] >> 4) & 15;
                     ml[j] = tok[j] & 15;
-                    off[j] = 0;
                     nx[j] = 0;
                 }
                 // literal length continuation (lz4.c:846-850): the first byte
@@ -809,11 +808,7 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                         else if (lit[j] > iend - ip[j] - (2 + 1 + kLastLiterals)) flags[j] = kTermIn;  // lz4.c:851
                     }
                     stat[j] = tok[j] >= 0 && flags[j] == 0;
-                    if (stat[j]) {
-                        const int ipo = ip[j] + lit[j];
-                        off[j] = (int)__ldg(src + ipo) | ((int)__ldg(src + ipo + 1) << 8);
-                        nx[j] = ipo + 2;
-                    }
+                    if (stat[j]) nx[j] = ip[j] + lit[j] + 2;  // the offset is read for real sequences only
                 }
                 // match length continuation (lz4.c:873-882)
 #pragma unroll
@@ -834,7 +829,7 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                     int t = kExit;
                     if (stat[j] && flags[j] == 0 && nx[j] - s0 < kWin) t = nx[j] - s0;
                     if (flags[j]) nx[j] = 0;
-                    cand[4 * lane + j] = make_int4(ip[j], lit[j], ml[j], off[j] | flags[j]);
+                    cand[4 * lane + j] = make_int4(ip[j], lit[j], ml[j], flags[j]);
                     nextp[4 * lane + j] = nx[j];
                     tword |= (uint32_t)t << (8 * j);
                 }
@@ -864,8 +859,11 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
                 q = cand[pos];
                 nx = nextp[pos];
             }
-            const int flags = q.w & ~0xffff, off = q.w & 0xffff;
+            const int flags = q.w & ~0xffff;
             const bool term_in = flags & kTermIn, slow = flags & kSlow;
+            const int off = member && !term_in && !slow
+                                ? (int)__ldg(src + q.x + q.y) | ((int)__ldg(src + q.x + q.y + 1) << 8)
+                                : 0;
             int len = member && !slow ? q.y + (term_in ? 0 : q.z) : 0;
             int incl = len;
 #pragma unroll
