@@ -356,14 +356,29 @@ __device__ __forceinline__ void runs_from_mask(const Shared &s)
     }
 }
 
-// n bytes from p into L2, one 128-byte line per thread and step (a hint:
-// nothing is read into registers)
-__device__ __forceinline__ void prefetch_l2_span(const uint8_t *p, int n)
+// n bytes from p into L2, one 128-byte line per thread and step, by
+// threads t of nt (a hint: nothing is read into registers)
+__device__ __forceinline__ void prefetch_l2_span(const uint8_t *p, int n, int t, int nt)
 {
     const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)127;
     const uintptr_t a1 = reinterpret_cast<uintptr_t>(p) + (uintptr_t)(n > 0 ? n : 0);
-    for (uintptr_t a = a0 + 128 * (uintptr_t)threadIdx.x; a < a1; a += 128 * (uintptr_t)blockDim.x)
+    for (uintptr_t a = a0 + 128 * (uintptr_t)t; a < a1; a += 128 * (uintptr_t)nt)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+}
+
+// A record's bytes into L2 (byte planes 1 and 2 from q12 when the LZ4 stage
+// left them in its input) by threads t of nt.
+__device__ __forceinline__ void prefetch_record(const uint8_t *slot, int nb, const uint8_t *q12, int t, int nt)
+{
+    const uint8_t *pay = slot + 4 + kMaskBytes;
+    const int np = nb - kMaskBytes, c4 = np / 4;
+    if (q12) {
+        prefetch_l2_span(slot, 4 + kMaskBytes + c4, t, nt);
+        prefetch_l2_span(q12, 2 * c4, t, nt);
+        prefetch_l2_span(pay + 3 * c4, np - 3 * c4, t, nt);
+    } else {
+        prefetch_l2_span(slot, 4 + nb, t, nt);
+    }
 }
 
 struct Payload {

@@ -206,41 +206,46 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const Shared s = carve(smem);
-    __shared__ long long s_ticket;
+    __shared__ long long s_ticket, s_next;
     __shared__ int s_bad;
+    // the next block's record, found by the last warp (s_pf_n < 0: none)
+    __shared__ const uint8_t *s_pf_slot, *s_pf_q12;
+    __shared__ int s_pf_n;
+    constexpr int kPfWarp = kNT / 32 - 1;
+    const int warp = threadIdx.x >> 5;
+    // byte planes 1 and 2 of block b's record in the LZ4 input (or null)
+    auto planes12 = [&](long long b, int nb) -> const uint8_t * {
+        if (!planes.hole || !shuffle) return nullptr;
+        const int c4 = (nb - kMaskBytes) / 4;
+        const int4 h = planes.hole[b];
+        return h.z > 0 && h.z == 2 * c4 && h.x == 4 + kMaskBytes + c4 ? planes.src + planes.src_off[b] + h.y
+                                                                       : nullptr;
+    };
 
+    // tickets are taken one block ahead, so that the next block's record
+    // can be brought into L2 while this one is transformed
+    if (threadIdx.x == 0) s_next = (long long)atomicAdd(queue, 1ull);
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
-            s_ticket = (long long)atomicAdd(queue, 1ull);
+            s_ticket = s_next;
+            s_next = s_next < total_blocks ? (long long)atomicAdd(queue, 1ull) : total_blocks;
             s_bad = 0;
         }
         __syncthreads();
         const long long g = s_ticket;
         if (g >= total_blocks) break;
+        const long long gn = s_next;
+        const long long ron = warp == kPfWarp && gn < total_blocks ? rec_off[gn] : -1;  // used after the load
         const BlockRef ref = locate(fields, nfields, g);
         const long long ro = rec_off[g];
         const uint8_t *slot = base + (ro < 0 ? 0 : ro);
         const int nb = ro < 0 ? -1 : *reinterpret_cast<const int *>(slot);
         const bool size_ok = nb >= kMaskBytes && nb <= kMaxRecord + 4;
-        // the payload into L2 while the mask is read and scanned (byte
-        // planes 1 and 2 from the LZ4 input where the LZ4 stage left them)
-        const uint8_t *q12 = nullptr;
-        if (size_ok) {
-            const uint8_t *pay = slot + 4 + kMaskBytes;
-            const int np = nb - kMaskBytes, c4 = np / 4;
-            if (planes.hole && shuffle) {
-                const int4 h = planes.hole[g];
-                if (h.z > 0 && h.z == 2 * c4 && h.x == 4 + kMaskBytes + c4) q12 = planes.src + planes.src_off[g] + h.y;
-            }
-            if (q12) {
-                prefetch_l2_span(pay, c4);
-                prefetch_l2_span(q12, 2 * c4);
-                prefetch_l2_span(pay + 3 * c4, np - 3 * c4);
-            } else {
-                prefetch_l2_span(pay, np);
-            }
-        }
+        // the payload into L2 while the mask is read and scanned (a no-op
+        // when the previous block's pass already brought it)
+        const uint8_t *q12 = size_ok ? planes12(g, nb) : nullptr;
+        if (size_ok) prefetch_record(slot, nb, q12, threadIdx.x, kNT);
         // deserialize_bitset (WaveletCompressor.cpp:124-150)
         for (int i = threadIdx.x; i < kMaskBytes / 4; i += kNT)
             s.mask32[i] = size_ok ? reinterpret_cast<const uint32_t *>(slot + 4)[i] : 0u;
@@ -273,6 +278,18 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
             for (int i = threadIdx.x; i < kBS3; i += kNT) s.sb[pidx(i & 31, (i >> 5) & 31, i >> 10)] = 0.f;
         }
         __syncthreads();
+        // the last warp finds the next record while level 8 runs on the
+        // first two warps
+        if (warp == kPfWarp) {
+            const int nbn = ron >= 0 ? *reinterpret_cast<const int *>(base + ron) : -1;
+            const bool okn = nbn >= kMaskBytes && nbn <= kMaxRecord + 4;
+            const uint8_t *qn = okn ? planes12(gn, nbn) : nullptr;
+            if ((threadIdx.x & 31) == 0) {
+                s_pf_slot = base + (ron < 0 ? 0 : ron);
+                s_pf_q12 = qn;
+                s_pf_n = okn ? nbn : -1;
+            }
+        }
         // ---- iwt: level 8 (x, z, y), level 16 (y, x, z), level 32 (z, y, x)
         sweep<8, 0, false, KIND>(s.sb);
         __syncthreads();
@@ -280,6 +297,8 @@ decode_kernel(const CzField *fields, int nfields, long long total_blocks, int sh
         __syncthreads();
         sweep<8, 1, false, KIND>(s.sb);
         __syncthreads();
+        // threads 256-511, idle during level 16, bring the next record into L2
+        if (threadIdx.x >= 256 && s_pf_n > 0) prefetch_record(s_pf_slot, s_pf_n, s_pf_q12, threadIdx.x - 256, kNT - 256);
         sweep<16, 1, false, KIND>(s.sb);
         __syncthreads();
         sweep<16, 0, false, KIND>(s.sb);
