@@ -693,6 +693,23 @@ __device__ __forceinline__ void copy_match(uint8_t *ring, int ms, int off, int m
         if (j < ml) ring[(ms + j) & kMask] = b[j];
 }
 
+// ml <= 8 bytes of a match at ms whose sources all lie before lo (in global
+// memory, or in the input where the hole is); r as in copy_match.
+__device__ __forceinline__ void copy_match_old(uint8_t *ring, int ms, int off, int ml, const uint8_t *src,
+                                               const uint8_t *dst, const LzHole &h)
+{
+    uint8_t b[8];
+    int r = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        b[j] = j < ml ? old_byte(src, dst, h, ms - off + r) : (uint8_t)0;
+        r = r + 1 == off ? 0 : r + 1;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (j < ml) ring[(ms + j) & kMask] = b[j];
+}
+
 // n bytes of the ring starting at ring offset r (r + n <= kRing) to d (any
 // alignment): 4-byte stores once d is aligned.
 __device__ __forceinline__ void flush(uint8_t *d, const uint8_t *ring, int r, int n, int lane)
@@ -924,8 +941,11 @@ lz4_decode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const
             // its lane, and when there is none, that first match replays
             // with the whole warp (long matches, sources in global memory)
             const int lo = max(ring_lo, op + kStage - kRing);  // not overwritten by this window
-            const bool fast = mat && q.z <= 8 && ms - off + min(q.z, off) <= op && ms - off >= lo;
-            if (fast) copy_match(ring, ms, off, q.z);
+            const bool fast_ring = mat && q.z <= 8 && ms - off + min(q.z, off) <= op && ms - off >= lo;
+            const bool fast_old = mat && q.z <= 8 && ms - off + min(q.z, off) <= lo;
+            const bool fast = fast_ring || fast_old;
+            if (fast_ring) copy_match(ring, ms, off, q.z);
+            else if (fast_old) copy_match_old(ring, ms, off, q.z, src, dst, hl);
             __syncwarp();
             bool todo = mat && !fast;
             pend = __ballot_sync(0xffffffffu, todo);
