@@ -9,13 +9,19 @@
 //     hash table of 1024 entries per warp in shared memory holds position
 //     (mod 2^18) and a 14-bit tag of the 4-byte sequence, so most false
 //     candidates are dropped without reading memory;
-//   * walk   -- lane k parses positions [32k, 32k+32) greedily, measuring
-//     matches against memory 16 bytes per round trip;
+//   * walk   -- lane k parses positions [16k, 16k+16) greedily, jumping
+//     from one position with a candidate to the next (a bitmask of its
+//     candidate slots) and measuring matches against memory;
 //   * merge  -- lane k keeps the sequences that start at or after the end
 //     of the last kept match of lanes < k (one ballot when no match crosses
 //     a later lane's last start, the exact serial rule otherwise);
 //   * emit   -- a warp scan places every kept sequence, each lane writes its
 //     own; literal runs over 32 bytes are copied by the whole warp.
+// Parse effort (a template level, cz_set_lz4_effort): 1 (default) extends
+// kept matches backwards over equal bytes (lz4.c's "catch up") and keeps
+// the tail of a match that a lower lane's match overlaps; 2 also takes
+// repeats at distance 1-3 that the table misses and starts each lane's
+// walk 8 positions early; 0 does neither.
 // Windows without a match advance faster after repeated misses (the
 // reference's acceleration idea, lz4.c:389-393). Chunks of block records
 // ([int32 nbytes][mask][4 byte planes], shuffle on) skip the search over
@@ -31,7 +37,12 @@
 // speculatively (every lane decodes tokens at 4 candidate positions; jump
 // tables by pointer doubling find the real sequences), output is staged in a
 // 4 KB per-warp ring and flushed with word stores; overlapping matches
-// repeat their first `offset` bytes, the byte-serial copy semantics.
+// repeat their first `offset` bytes, the byte-serial copy semantics. Short
+// matches are copied by their own lanes in rounds (sources before the
+// window first, then those whose sources the earlier rounds completed);
+// long ones by the whole warp. For one-record chunks of shuffled records a
+// literal run that covers byte planes 1 and 2 whole stays in the input
+// (hole), where later matches and the decode kernel read it.
 #include "cz_codec.h"
 #include "cz_deflate.cuh"
 
