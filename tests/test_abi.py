@@ -65,3 +65,11 @@ def test_noalloc_pointer_checks_precede_any_cuda_call(lib):
     for nb in (0, -1, _lib.NOALLOC_MAX_BLOCKS + 1):
         assert f(C.c_void_p(ok_b), nb, C.c_float(0.0), 1, 0, 0, C.c_void_p(ok_r), C.c_void_p(ok_n),
                  None) == _lib.CZ_E_ARG
+
+
+def test_lz4_effort_needs_a_context(lib):
+    """cz_set_lz4_effort checks its arguments before anything else: a NULL
+    context is refused with CZ_E_ARG whatever the level."""
+    from cubismz_gb300 import _lib
+    for level in (-1, 0, 1, 2, 3):
+        assert lib.cz_set_lz4_effort(None, level) == _lib.CZ_E_ARG
