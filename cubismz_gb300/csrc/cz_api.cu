@@ -1236,11 +1236,11 @@ int cz_compress_to_image(cz_ctx *c, const float *h_field, int nx, int ny, int nz
             cudaStream_t ls = c->s_lz[i];
             CZ_CUDA(c, cudaStreamWaitEvent(ls, c->ev_enc[i], 0));
             uint8_t *lzo = P<uint8_t>(c->lz_out) + f0 * job.lz_slot;
-            // whole-SM CTAs (32 chunks each): LZ4 and the wavelet kernel of
+            // whole-SM CTAs (16 chunks each): LZ4 and the wavelet kernel of
             // the next slabs then share the GPU SM by SM
-            const int lzgrid = std::max(1, std::min((n + 31) / 32, c->sms));
+            const int lzgrid = std::max(1, std::min((n + 15) / 16, c->sms));
             CZ_CUDA(c, cz_launch_lz4_encode(stage, src_off, len, n, lzo, P<long long>(c->lz_off) + f0,
-                                            P<int>(c->lz_len) + f0, p->shuffle ? 1 : 0, 32, lzgrid, ls,
+                                            P<int>(c->lz_len) + f0, p->shuffle ? 1 : 0, 16, lzgrid, ls,
                                             P<int4>(c->lz_hole) + f0, c->lz_effort));
             CZ_CUDA(c, cz_launch_neg_reduce(P<int>(c->lz_len) + f0, n, P<int>(c->flag), ls));
             CZ_CUDA(c, cudaEventRecord(c->ev_lz[i], ls));

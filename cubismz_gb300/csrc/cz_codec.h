@@ -59,7 +59,7 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 // bytes past its end (buffers carry tail room). Outputs may start anywhere.
 // records != 0: chunks hold block records with shuffled byte planes; the
 // search skips planes 1 and 2 (copied as literals).
-// warps: 2, 4, 8, 16 or 32 warps (chunks) per CTA (32 fills an SM); any
+// warps: 2, 4, 8 or 16 warps (chunks) per CTA (16 takes an SM); any
 // choice gives the same bytes.
 // hole (optional): written for every chunk, {out position, input position,
 // length, 0} of one literal-only span (byte planes 1 and 2 of a record

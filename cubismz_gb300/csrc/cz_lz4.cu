@@ -4,12 +4,12 @@
 // LZ4_uncompress_unknownOutputSize (ThirdParty/lz4/lz4.c:802-905): minimum
 // match 4, offsets 1..65535, the last 5 bytes are literals and the last
 // match starts at least 12 bytes before the end (lz4.c:177-204). A warp
-// takes super-windows of 512 positions:
+// takes super-windows of 512 or 768 positions (see window_for):
 //   * probe  -- 4 positions per lane per step from coalesced word loads; a
 //     hash table of 1024 entries per warp in shared memory holds position
 //     (mod 2^18) and a 14-bit tag of the 4-byte sequence, so most false
 //     candidates are dropped without reading memory;
-//   * walk   -- lane k parses positions [16k, 16k+16) greedily, jumping
+//   * walk   -- lane k parses its 16 or 24 positions greedily, jumping
 //     from one position with a candidate to the next (a bitmask of its
 //     candidate slots) and measuring matches against memory;
 //   * merge  -- lane k keeps the sequences that start at or after the end
@@ -177,7 +177,11 @@ __device__ __forceinline__ void next_skip(Skip &k, const uint8_t *src, int L)
 //   emit   -- every lane sizes its kept sequences, a warp scan places them,
 //             every lane writes its own; literal runs longer than 32 bytes
 //             are queued and copied by the whole warp.
-constexpr int kSW = 512, kSub = kSW / 32, kMaxSeqLane = kSub / 4, kOvl = 8;
+constexpr int kOvl = 8;
+// super-window sizes: 768 positions when every chunk of the launch is
+// resident at once (fewer windows per chunk), 512 otherwise (a smaller
+// per-warp footprint, so more chunks share an SM)
+constexpr int kWinSmall = 512, kWinLarge = 768;
 constexpr int kMinHole = 256;  // smallest literal-only span left to the gather
 // Hash table entry: position modulo 2^18 in the high bits, a 14-bit tag of
 // the 4-byte sequence in the low bits. A tag hit is only a candidate: the
@@ -255,24 +259,27 @@ __device__ __forceinline__ int match_len_back(const uint8_t *src, int p, int can
 // to 32 KiB, and per kept sequence one 8-byte record (literal run, match
 // length, distance; zl::seq_pack) at out + out_off[c]; the last record holds
 // the tail literals. out_len[c] = record bytes, -1 past the capacity.
-// Shared memory of one encoder warp (dynamic shared memory, one per warp).
+// Shared memory of one encoder warp for super-windows of SW positions.
+template <int SW>
 struct LzEncWarp {
     uint32_t table[1 << kHashLog];
     int4 longq[32];                   // (dst offset, src offset, n, -)
-    uint32_t seq[32][kMaxSeqLane];    // start - base | back extension << 12 | offset << 16
-    int lens[32][kMaxSeqLane];
-    uint16_t info[kSW];               // candidate offset per position, 0: none
+    uint32_t seq[32][SW / 128];       // start - base | back extension << 12 | offset << 16
+    int lens[32][SW / 128];
+    uint16_t info[SW];                // candidate offset per position, 0: none
     int nlong;
 };
 
-template <int kLzWarps, bool SEQ, int kEffort>
+template <int kLzWarps, bool SEQ, int kEffort, int kSW>
 __global__ void __launch_bounds__(kLzWarps * 32)
 lz4_encode_kernel(const uint8_t *__restrict__ in, const long long *in_off, const int *in_len, int nchunks,
                   uint8_t *__restrict__ out, const long long *out_off, int *out_len, int records, int4 *hole)
 {
+    constexpr int kSub = kSW / 32, kMaxSeqLane = kSub / 4;  // positions and sequences per lane
+    using LzEncWarp = cz::LzEncWarp<kSW>;
     constexpr bool kThorough = kEffort >= 2;
     constexpr int kMaxOff = SEQ ? zl::kMaxDist : 65535;
-    // up to 8 warps in static shared memory; 32 (a whole SM) in dynamic
+    // up to 8 warps in static shared memory; 16 in dynamic
     extern __shared__ __align__(16) unsigned char lz_enc_smem[];
     __shared__ LzEncWarp lz_enc_static[kLzWarps <= 8 ? kLzWarps : 1];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1106,16 +1113,16 @@ __global__ void gather_kernel(const uint8_t *__restrict__ src, const long long *
 
 using namespace cz;
 
-// kLzWarps chunks per CTA; 32 fills an SM (1024 threads, ~210 KB of shared
-// memory), so that CTAs of this kernel and the wavelet kernel, which also
-// takes a whole SM, share the machine SM by SM.
-template <int W, bool SEQ, int E>
+// kLzWarps chunks per CTA; 16 (512 threads, ~123 KB of shared memory)
+// takes an SM, so that CTAs of this kernel and the wavelet kernel, which
+// also takes a whole SM, share the machine SM by SM.
+template <int W, bool SEQ, int E, int SW>
 static cudaError_t launch_enc_t(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                                 uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
                                 cudaStream_t st, int4 *hole)
 {
-    const int sm = W <= 8 ? 0 : (int)sizeof(LzEncWarp) * W;
-    auto k = lz4_encode_kernel<W, SEQ, E>;
+    const int sm = W <= 8 ? 0 : (int)sizeof(LzEncWarp<SW>) * W;
+    auto k = lz4_encode_kernel<W, SEQ, E, SW>;
     if (sm > 48 * 1024) {
         const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         if (e != cudaSuccess) return e;
@@ -1125,19 +1132,47 @@ static cudaError_t launch_enc_t(const uint8_t *in, const long long *in_off, cons
 }
 
 // one kernel per effort level, so that a level pays only for its own work
+template <int W, bool SEQ, int SW>
+static cudaError_t launch_enc_e(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
+                                uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
+                                cudaStream_t st, int4 *hole, int effort)
+{
+    switch (effort) {
+    case 0:
+        return launch_enc_t<W, SEQ, 0, SW>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st,
+                                           hole);
+    case 2:
+        return launch_enc_t<W, SEQ, 2, SW>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st,
+                                           hole);
+    default:
+        return launch_enc_t<W, SEQ, 1, SW>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st,
+                                           hole);
+    }
+}
+
+// The super-window size depends only on the chunk count and the GPU, so
+// that every CTA width writes the same bytes: 768 positions when all chunks
+// fit on the SMs at once with 4 chunks per CTA (7 CTAs of 4 warps per SM),
+// else 512.
+static int window_for(int nchunks)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                   cudaSuccess)
+        sms = 1;
+    return (long long)nchunks <= 28LL * sms ? kWinLarge : kWinSmall;
+}
+
 template <int W, bool SEQ>
 static cudaError_t launch_enc(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
                               uint8_t *out, const long long *out_off, int *out_len, int records, int grid,
                               cudaStream_t st, int4 *hole, int effort)
 {
-    switch (effort) {
-    case 0:
-        return launch_enc_t<W, SEQ, 0>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
-    case 2:
-        return launch_enc_t<W, SEQ, 2>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
-    default:
-        return launch_enc_t<W, SEQ, 1>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole);
-    }
+    if (window_for(nchunks) == kWinLarge)
+        return launch_enc_e<W, SEQ, kWinLarge>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st,
+                                               hole, effort);
+    return launch_enc_e<W, SEQ, kWinSmall>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st,
+                                           hole, effort);
 }
 
 cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, const int *in_len, int nchunks,
@@ -1152,8 +1187,6 @@ cudaError_t cz_launch_lz4_encode(const uint8_t *in, const long long *in_off, con
         return launch_enc<8, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
     case 16:
         return launch_enc<16, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
-    case 32:
-        return launch_enc<32, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
     default:
         return launch_enc<4, false>(in, in_off, in_len, nchunks, out, out_off, out_len, records, grid, st, hole, effort);
     }
