@@ -60,7 +60,8 @@ cudaError_t cz_launch_refit(int wtype, const CzField *fields, int nfields, long 
 // records != 0: chunks hold block records with shuffled byte planes; the
 // search skips planes 1 and 2 (copied as literals).
 // warps: 2, 4, 8 or 16 warps (chunks) per CTA (16 takes an SM); any
-// choice gives the same bytes.
+// choice gives the same bytes (the parse's super-window, 512 or 768
+// positions, follows from nchunks and the SM count alone).
 // hole (optional): written for every chunk, {out position, input position,
 // length, 0} of one literal-only span (byte planes 1 and 2 of a record
 // chunk) that the encoder leaves unwritten in its output for the gather to
